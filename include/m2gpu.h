@@ -1,0 +1,131 @@
+/*
+ * m2gpu.h -- C ABI of the GB300 Lucas-Lehmer / PRP engine (libm2gpu.so).
+ *
+ * The reference (cherubrock-seb/mersenne2GPU) is one executable: main() owns
+ * the OpenCL context, the device buffers z / w / iw / digit_width / blocks /
+ * states / carry (mersenne2_gpu.cpp:4010-4028), enqueues an iteration plan p
+ * (PRP) or p-2 (LL) times (mersenne2_gpu.cpp:4812-4822) and reads z back once
+ * to decide (mersenne2_gpu.cpp:4855-4882).  There is no plugin or FFI API; the
+ * entry points below are what its per-iteration contract becomes as a library.
+ * The mersenne2 CLI of this project (mersenne2gpu_gb300/csrc/mersenne2_cli.cpp)
+ * keeps the reference's command line and output on top of them.
+ *
+ * Conventions: every function returns 0 or a negative M2_E* code and never
+ * exits or traps; device waits are bounded.  A context owns all device memory
+ * it uses, the caller owns host buffers.  Calls on one context are not
+ * thread-safe; different contexts are independent.  Digits are the residue's
+ * n words of width q or q+1 bits (q = p >> log2 n), least significant first,
+ * each in [0, 2^width): the same layout as the reference's z[k].s0 / z[k].s1
+ * after its carry (mersenne2_gpu.cpp:2116, 3400-3410).
+ */
+#ifndef M2GPU_H
+#define M2GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* test modes: LL and PRP as in mersenne2_gpu.cpp:3454-3462 (TestMode);
+ * PRP3 (x <- 3 x^2, p-1 steps, prime iff 3) as in the GF61 prototype
+ * gf61_ntt_prp_opencl_inplace_nobitrev_fused.cpp:508-531. */
+enum { M2_MODE_LL = 0, M2_MODE_PRP = 1, M2_MODE_PRP3 = 2 };
+
+/* execution path selection (0 = automatic) */
+enum { M2_PATH_AUTO = 0, M2_PATH_SMALL = 1, M2_PATH_LARGE = 2 };
+
+enum {
+    M2_OK = 0,
+    M2_EINVAL = -1,       /* bad argument (reference: usage error, exit 1, mersenne2_gpu.cpp:3618-3716) */
+    M2_ENOMEM = -2,       /* device allocation failed */
+    M2_ECUDA = -3,        /* CUDA runtime error (reference: check() -> exit(1), mersenne2_gpu.cpp:3078-3083) */
+    M2_ETIMEOUT = -4,     /* a bounded device wait gave up */
+    M2_ESTATE = -5,       /* a kernel reported an out-of-range carry / normalization failure */
+    M2_EUNSUPPORTED = -6  /* exponent or option outside what this build supports */
+};
+
+typedef struct m2_ctx m2_ctx;
+
+/* Options; zero-initialise and set what you need.  The -W / -B knobs of the
+ * reference (mersenne2_gpu.cpp:3668-3680) are accepted: wg is the threads per
+ * CTA hint, carry_pairs the carry segment size hint (pairs of digits). */
+typedef struct {
+    int device;             /* CUDA device ordinal (reference -d, mersenne2_gpu.cpp:3651-3656) */
+    uint32_t wg;            /* -W: threads per CTA hint (0 = auto) */
+    uint32_t carry_pairs;   /* -B: carry segment length hint in digit pairs (0 = auto) */
+    int path;               /* M2_PATH_* */
+    void* stream;           /* cudaStream_t to run on (NULL = the context creates one) */
+} m2_opts;
+
+typedef struct {
+    uint32_t p;
+    int mode;
+    int ln;                 /* log2 n, the reference's transformsize (mersenne2_gpu.cpp:286-293) */
+    uint64_t n;             /* digits */
+    uint32_t iteration;     /* squarings applied so far */
+    uint32_t total_iters;   /* p-2 (LL), p (PRP), p-1 (PRP3) (mersenne2_gpu.cpp:4780) */
+    int path;               /* M2_PATH_SMALL or M2_PATH_LARGE */
+    uint32_t rows, row_len, cols_per_cta, span;   /* large-path plan */
+    uint64_t device_bytes;  /* device memory held by the context */
+} m2_info_t;
+
+/* Replaces main()'s setup (mersenne2_gpu.cpp:3727-4028): exponent -> transform,
+ * tables, buffers, x0 = 4 (LL) / 3 (PRP, PRP3) (mersenne2_gpu.cpp:3908). */
+int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts);
+
+/* Replaces k rounds of enqueue_plan(iter_plan); enqueue_plan(post_plan);
+ * (mersenne2_gpu.cpp:4812-4822).  Asynchronous on the context's stream. */
+int m2_iterate(m2_ctx* ctx, uint32_t k);
+
+/* Replaces clFinish at a report point (mersenne2_gpu.cpp:4788); also reports
+ * device-side status (M2_ESTATE). */
+int m2_sync(m2_ctx* ctx);
+
+/* Replaces the final clEnqueueReadBuffer of z (mersenne2_gpu.cpp:4855-4863):
+ * n canonical digits; the all-ones vector (== M_p) is returned as zero. */
+int m2_get_digits(m2_ctx* ctx, uint64_t* out);
+
+/* Sets the state from n digits (any values with digit_j < 2^64; the residue
+ * is sum digit_j 2^bitpos_j mod M_p) and the iteration counter (resume). */
+int m2_set_digits(m2_ctx* ctx, const uint64_t* digits, uint32_t iteration);
+
+/* Low 64 bits of the canonical residue (the reference prints none; added). */
+int m2_res64(m2_ctx* ctx, uint64_t* out);
+
+/* Verdict of the current state: 1 = prime / probable prime, 0 = composite.
+ * LL: residue 0 (mersenne2_gpu.cpp:3028-3042); PRP: residue 9
+ * (mersenne2_gpu.cpp:3051-3076); PRP3: residue 3. */
+int m2_verdict(m2_ctx* ctx, int* is_prime);
+
+int m2_info(m2_ctx* ctx, m2_info_t* info);
+
+/* Releases everything the context owns (mersenne2_gpu.cpp:4884-4958). */
+void m2_destroy(m2_ctx* ctx);
+
+/* Digit widths (n bytes) of exponent p, without a device; and log2 n. */
+int m2_layout(uint32_t p, int* ln, uint64_t* n, uint8_t* widths /* may be NULL */);
+
+const char* m2_strerror(int code);
+
+/* ---------------- batched engine ----------------
+ * Runs `count` independent tests to completion (or `iters[i]` squarings when
+ * iters != NULL) in persistent launches grouped by transform size, one CTA per
+ * test.  res64_out[i] and is_prime_out[i] (may be NULL) receive the results.
+ * No reference counterpart: the reference runs one exponent per process
+ * (mersenne2_gpu.cpp:3618-4959). */
+typedef struct {
+    double seconds;          /* device time of the launches */
+    uint64_t squarings;      /* total squarings performed */
+    uint32_t launches;       /* kernel launches issued */
+    uint32_t buckets;        /* distinct transform sizes */
+} m2_batch_stats;
+
+int m2_batch_run(const uint32_t* p, const int* modes, const uint32_t* iters, size_t count,
+                 uint64_t* res64_out, int* is_prime_out, int device, m2_batch_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* M2GPU_H */

@@ -1,0 +1,213 @@
+"""GB300-native Lucas-Lehmer / PRP engine for Mersenne numbers 2^p - 1.
+
+Python binding of the C ABI in include/m2gpu.h (libm2gpu.so, built in-tree by
+mersenne2gpu_gb300.build).  There is no CPU fallback: every call runs the CUDA
+kernels, and importing the binding raises if the library was not built.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libm2gpu.so")
+
+MODE_LL, MODE_PRP, MODE_PRP3 = 0, 1, 2
+PATH_AUTO, PATH_SMALL, PATH_LARGE = 0, 1, 2
+_MODES = {"ll": MODE_LL, "prp": MODE_PRP, "prp3": MODE_PRP3}
+
+# every symbol include/m2gpu.h declares
+EXPORTS = (
+    "m2_create", "m2_iterate", "m2_sync", "m2_get_digits", "m2_set_digits", "m2_res64",
+    "m2_verdict", "m2_info", "m2_destroy", "m2_layout", "m2_strerror", "m2_batch_run",
+)
+
+
+class M2Error(RuntimeError):
+    def __init__(self, code: int, what: str):
+        super().__init__(f"{what}: {_lib().m2_strerror(code).decode()} ({code})")
+        self.code = code
+
+
+class _Opts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("wg", ctypes.c_uint32), ("carry_pairs", ctypes.c_uint32),
+                ("path", ctypes.c_int), ("stream", ctypes.c_void_p)]
+
+
+class _Info(ctypes.Structure):
+    _fields_ = [("p", ctypes.c_uint32), ("mode", ctypes.c_int), ("ln", ctypes.c_int), ("n", ctypes.c_uint64),
+                ("iteration", ctypes.c_uint32), ("total_iters", ctypes.c_uint32), ("path", ctypes.c_int),
+                ("rows", ctypes.c_uint32), ("row_len", ctypes.c_uint32), ("cols_per_cta", ctypes.c_uint32),
+                ("span", ctypes.c_uint32), ("device_bytes", ctypes.c_uint64)]
+
+
+class _BatchStats(ctypes.Structure):
+    _fields_ = [("seconds", ctypes.c_double), ("squarings", ctypes.c_uint64), ("launches", ctypes.c_uint32),
+                ("buckets", ctypes.c_uint32)]
+
+
+_LIB = None
+
+
+def _lib() -> ctypes.CDLL:
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -m mersenne2gpu_gb300.build` first")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, u32, u64, i = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+        L.m2_create.argtypes = [ctypes.POINTER(vp), u32, i, ctypes.POINTER(_Opts)]
+        L.m2_iterate.argtypes = [vp, u32]
+        L.m2_sync.argtypes = [vp]
+        L.m2_get_digits.argtypes = [vp, vp]
+        L.m2_set_digits.argtypes = [vp, vp, u32]
+        L.m2_res64.argtypes = [vp, ctypes.POINTER(u64)]
+        L.m2_verdict.argtypes = [vp, ctypes.POINTER(i)]
+        L.m2_info.argtypes = [vp, ctypes.POINTER(_Info)]
+        L.m2_destroy.argtypes = [vp]
+        L.m2_destroy.restype = None
+        L.m2_layout.argtypes = [u32, ctypes.POINTER(i), ctypes.POINTER(u64), vp]
+        L.m2_strerror.argtypes = [i]
+        L.m2_strerror.restype = ctypes.c_char_p
+        L.m2_batch_run.argtypes = [vp, vp, vp, ctypes.c_size_t, vp, vp, i, ctypes.POINTER(_BatchStats)]
+        for name in EXPORTS:
+            if name not in ("m2_destroy", "m2_strerror"):
+                getattr(L, name).restype = i
+        _LIB = L
+    return _LIB
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise M2Error(rc, what)
+
+
+def layout(p: int) -> tuple[int, int, np.ndarray]:
+    """(log2 n, n, digit widths) of exponent p; no device needed."""
+    L = _lib()
+    ln, n = ctypes.c_int(), ctypes.c_uint64()
+    _check(L.m2_layout(p, ctypes.byref(ln), ctypes.byref(n), None), "m2_layout")
+    w = np.zeros(n.value, dtype=np.uint8)
+    _check(L.m2_layout(p, ctypes.byref(ln), ctypes.byref(n), w.ctypes.data), "m2_layout")
+    return ln.value, n.value, w
+
+
+def total_iterations(p: int, mode: int) -> int:
+    return {MODE_LL: p - 2, MODE_PRP: p, MODE_PRP3: p - 1}[mode]
+
+
+@dataclass
+class Info:
+    p: int
+    mode: int
+    ln: int
+    n: int
+    iteration: int
+    total_iters: int
+    path: int
+    rows: int
+    row_len: int
+    cols_per_cta: int
+    span: int
+    device_bytes: int
+
+
+class Engine:
+    """One test of 2^p - 1 on one GPU (wraps an m2_ctx)."""
+
+    def __init__(self, p: int, mode: int | str = MODE_PRP, device: int = 0, path: int = PATH_AUTO,
+                 wg: int = 0, carry_pairs: int = 0, stream: int | None = None):
+        if isinstance(mode, str):
+            mode = _MODES[mode.lower()]
+        self._L = _lib()
+        self._h = ctypes.c_void_p()
+        o = _Opts(device, wg, carry_pairs, path, stream)
+        _check(self._L.m2_create(ctypes.byref(self._h), p, mode, ctypes.byref(o)), f"m2_create(p={p})")
+        self.p, self.mode = p, mode
+        self.info()
+
+    def close(self) -> None:
+        if self._h:
+            self._L.m2_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> Info:
+        i = _Info()
+        _check(self._L.m2_info(self._h, ctypes.byref(i)), "m2_info")
+        self.n = i.n
+        return Info(i.p, i.mode, i.ln, i.n, i.iteration, i.total_iters, i.path, i.rows, i.row_len,
+                    i.cols_per_cta, i.span, i.device_bytes)
+
+    def iterate(self, k: int) -> None:
+        _check(self._L.m2_iterate(self._h, k), "m2_iterate")
+
+    def sync(self) -> None:
+        _check(self._L.m2_sync(self._h), "m2_sync")
+
+    def digits(self) -> np.ndarray:
+        out = np.zeros(self.n, dtype=np.uint64)
+        _check(self._L.m2_get_digits(self._h, out.ctypes.data), "m2_get_digits")
+        return out
+
+    def set_digits(self, d: np.ndarray, iteration: int) -> None:
+        d = np.ascontiguousarray(d, dtype=np.uint64)
+        if d.shape != (self.n,):
+            raise ValueError(f"expected {self.n} digits")
+        _check(self._L.m2_set_digits(self._h, d.ctypes.data, iteration), "m2_set_digits")
+
+    def res64(self) -> int:
+        r = ctypes.c_uint64()
+        _check(self._L.m2_res64(self._h, ctypes.byref(r)), "m2_res64")
+        return r.value
+
+    def verdict(self) -> bool:
+        v = ctypes.c_int()
+        _check(self._L.m2_verdict(self._h, ctypes.byref(v)), "m2_verdict")
+        return bool(v.value)
+
+    def run(self) -> bool:
+        """Remaining iterations to completion; returns the verdict."""
+        i = self.info()
+        self.iterate(i.total_iters - i.iteration)
+        return self.verdict()
+
+
+@dataclass
+class BatchResult:
+    res64: np.ndarray
+    is_prime: np.ndarray
+    seconds: float
+    squarings: int
+    launches: int
+    buckets: int
+
+
+def batch_run(ps, modes=None, iters=None, device: int = 0) -> BatchResult:
+    """Independent tests in bucketed persistent launches (m2_batch_run)."""
+    L = _lib()
+    p = np.ascontiguousarray(ps, dtype=np.uint32)
+    cnt = len(p)
+    m = None if modes is None else np.ascontiguousarray(
+        [(_MODES[x] if isinstance(x, str) else x) for x in modes], dtype=np.int32)
+    it = None if iters is None else np.ascontiguousarray(iters, dtype=np.uint32)
+    res = np.zeros(cnt, dtype=np.uint64)
+    pr = np.zeros(cnt, dtype=np.int32)
+    st = _BatchStats()
+    _check(L.m2_batch_run(p.ctypes.data, None if m is None else m.ctypes.data, None if it is None else it.ctypes.data,
+                          cnt, res.ctypes.data, pr.ctypes.data, device, ctypes.byref(st)), "m2_batch_run")
+    return BatchResult(res, pr.astype(bool), st.seconds, st.squarings, st.launches, st.buckets)

@@ -1,0 +1,479 @@
+// m2_api.cu -- the C ABI of include/m2gpu.h on top of the kernels.
+#include "../../include/m2gpu.h"
+#include "m2_host.hpp"
+#include "m2_kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <stdexcept>
+#include <tuple>
+#include <vector>
+
+using m2::i64;
+using m2::u32;
+using m2::u64;
+
+namespace {
+
+// ---------------- device twiddle cache (one table set per device and h) ----------------
+struct TwTables {
+    m2k::DTw* tw4 = nullptr;
+    m2k::DTw* tc = nullptr;
+    size_t bytes = 0;
+};
+std::mutex g_tw_mu;
+std::map<std::pair<int, u64>, TwTables> g_tw;
+
+int get_twiddles(int device, u64 h, TwTables& out) {
+    std::lock_guard<std::mutex> lk(g_tw_mu);
+    auto it = g_tw.find({device, h});
+    if (it != g_tw.end()) { out = it->second; return M2_OK; }
+    m2::Twiddles T = m2::make_twiddles(h);
+    TwTables t;
+    const size_t b4 = T.tw4.size() * sizeof(m2::Dual), bc = T.tc.size() * sizeof(m2::Dual);
+    if (cudaMalloc(&t.tw4, b4) != cudaSuccess) return M2_ENOMEM;
+    if (cudaMalloc(&t.tc, bc) != cudaSuccess) { cudaFree(t.tw4); return M2_ENOMEM; }
+    if (cudaMemcpy(t.tw4, T.tw4.data(), b4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(t.tc, T.tc.data(), bc, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(t.tw4); cudaFree(t.tc);
+        return M2_ECUDA;
+    }
+    t.bytes = b4 + bc;
+    g_tw[{device, h}] = t;
+    out = t;
+    return M2_OK;
+}
+
+u32 total_iters_for(u32 p, int mode) {
+    if (mode == M2_MODE_LL) return p >= 2 ? p - 2 : 0;
+    if (mode == M2_MODE_PRP3) return p - 1;
+    return p;
+}
+
+// Carry threads of the one-CTA path: a power of two, each owning n/Tc >= span+1
+// digits; 0 selects the single-thread full normalization (tiny exponents).
+int small_carry_threads(const m2::Layout& L, int span, int threads) {
+    if (L.q < 4) return 0;
+    u64 tc = (u64)threads;
+    while (tc > 1 && L.n / tc < (u64)span + 1) tc >>= 1;
+    if (L.n / tc < (u64)span + 1) return 0;
+    return (int)tc;
+}
+
+}  // namespace
+
+struct m2_ctx {
+    m2::Layout L;
+    int mode = M2_MODE_PRP;
+    int path = M2_PATH_SMALL;
+    u32 iteration = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int span = 0;
+    uint64_t bytes = 0;
+    // tables
+    unsigned char* d_w61 = nullptr;
+    unsigned char* d_w31 = nullptr;
+    TwTables tw;
+    int* d_status = nullptr;
+    long long* d_digits = nullptr;
+    // small path
+    m2k::SmallTest* d_test = nullptr;
+    int threads = 0;
+    int carry_threads = 0;
+    // large path
+    m2k::LargePlan plan{};
+    m2k::LargeBufs bufs{};
+    long long* d_carries = nullptr;
+    ulonglong2* d_za = nullptr;
+    uint2* d_zb = nullptr;
+};
+
+namespace {
+
+template <class T> int dalloc(m2_ctx* c, T** p, size_t bytes) {
+    if (cudaMalloc((void**)p, bytes) != cudaSuccess) { cudaGetLastError(); return M2_ENOMEM; }
+    c->bytes += bytes;
+    return M2_OK;
+}
+
+bool plan_large(const m2::Layout& L, int span, u32 carry_pairs, m2k::LargePlan& P) {
+    const int Lh = L.ln - 1;
+    if (Lh < 6) return false;
+    int L1 = 2 * (Lh / 4);
+    if (L1 < 2) L1 = 2;
+    const int L2 = Lh - L1;
+    P.ln = L.ln; P.L = Lh; P.L1 = L1; P.L2 = L2;
+    P.R = 1u << L1; P.B = 1u << L2;
+    P.span = span; P.p = L.p;
+    u32 C = 16;
+    while (C > 4 && 24ull * C * P.R > 100 * 1024) C >>= 1;
+    if (carry_pairs >= 4 && carry_pairs <= 16 && (carry_pairs & (carry_pairs - 1)) == 0) C = carry_pairs;
+    while (2 * C < (u32)span + 1 && C < 16) C <<= 1;
+    if (2 * C < (u32)span + 1 || C > P.B) return false;
+    P.C = C; P.G = P.B / C;
+    return true;
+}
+
+int cuda_err(cudaError_t e) { return e == cudaSuccess ? M2_OK : (e == cudaErrorMemoryAllocation ? M2_ENOMEM : M2_ECUDA); }
+
+int upload_state(m2_ctx* c, const std::vector<u64>& canon) {
+    std::vector<i64> bal = m2::balanced_digits(c->L, canon);
+    cudaError_t e = cudaMemcpyAsync(c->d_digits, bal.data(), bal.size() * sizeof(i64), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess && c->path == M2_PATH_LARGE)
+        e = cudaMemsetAsync(c->d_carries, 0, sizeof(i64) * (size_t)c->plan.R * c->plan.G, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return cuda_err(e);
+}
+
+int read_canonical(m2_ctx* c, std::vector<u64>& out) {
+    int rc = m2_sync(c);
+    if (rc) return rc;
+    std::vector<i64> d(c->L.n);
+    std::vector<i64> car;
+    cudaError_t e = cudaMemcpy(d.data(), c->d_digits, d.size() * sizeof(i64), cudaMemcpyDeviceToHost);
+    u64 seg = 0;
+    if (e == cudaSuccess && c->path == M2_PATH_LARGE) {
+        car.resize((size_t)c->plan.R * c->plan.G);
+        e = cudaMemcpy(car.data(), c->d_carries, car.size() * sizeof(i64), cudaMemcpyDeviceToHost);
+        seg = 2ull * c->plan.C;
+    }
+    if (e != cudaSuccess) return M2_ECUDA;
+    try {
+        out = m2::canonical_digits(c->L, d, car, seg);
+    } catch (const std::exception&) {
+        return M2_ESTATE;
+    }
+    return M2_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* m2_strerror(int code) {
+    switch (code) {
+        case M2_OK: return "ok";
+        case M2_EINVAL: return "invalid argument";
+        case M2_ENOMEM: return "out of device memory";
+        case M2_ECUDA: return "CUDA runtime error";
+        case M2_ETIMEOUT: return "device wait timed out";
+        case M2_ESTATE: return "device reported an out-of-range carry";
+        case M2_EUNSUPPORTED: return "unsupported exponent or option";
+        default: return "unknown error";
+    }
+}
+
+int m2_layout(uint32_t p, int* ln, uint64_t* n, uint8_t* widths) {
+    if (p < 3) return M2_EINVAL;
+    m2::Layout L = m2::make_layout(p);
+    if (ln) *ln = L.ln;
+    if (n) *n = L.n;
+    if (widths) std::memcpy(widths, L.width.data(), L.n);
+    return M2_OK;
+}
+
+int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
+    if (!out) return M2_EINVAL;
+    *out = nullptr;
+    if (p < 3 || mode < M2_MODE_LL || mode > M2_MODE_PRP3) return M2_EINVAL;
+    m2_opts o{};
+    if (opts) o = *opts;
+    if (m2::transform_log2(p) > 30) return M2_EUNSUPPORTED;
+    std::unique_ptr<m2_ctx> c(new (std::nothrow) m2_ctx());
+    if (!c) return M2_ENOMEM;
+    c->L = m2::make_layout(p);
+    c->mode = mode;
+    c->device = o.device;
+    if (cudaSetDevice(o.device) != cudaSuccess) { cudaGetLastError(); return M2_EINVAL; }
+    c->span = m2::carry_span(c->L);
+    const u64 h = c->L.h;
+    int path = o.path;
+    if (path == M2_PATH_AUTO) path = (h <= 8192) ? M2_PATH_SMALL : M2_PATH_LARGE;
+    if (path == M2_PATH_SMALL && h > 8192) return M2_EUNSUPPORTED;
+    if (path == M2_PATH_LARGE && !plan_large(c->L, c->span, o.carry_pairs, c->plan)) return M2_EUNSUPPORTED;
+    c->path = path;
+    if (o.stream) { c->stream = (cudaStream_t)o.stream; }
+    else {
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return M2_ECUDA;
+        c->own_stream = true;
+    }
+    int rc;
+    const u64 n = c->L.n;
+    if ((rc = get_twiddles(c->device, h, c->tw))) { m2_destroy(c.release()); return rc; }
+    m2_ctx* raw = c.get();
+    if ((rc = dalloc(raw, &raw->d_w61, n)) || (rc = dalloc(raw, &raw->d_w31, n)) ||
+        (rc = dalloc(raw, &raw->d_status, sizeof(int))) || (rc = dalloc(raw, &raw->d_digits, n * sizeof(i64)))) {
+        m2_destroy(c.release());
+        return rc;
+    }
+    cudaError_t e = cudaMemcpy(raw->d_w61, raw->L.w61.data(), n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(raw->d_w31, raw->L.w31.data(), n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(raw->d_status, 0, sizeof(int));
+    if (e != cudaSuccess) { m2_destroy(c.release()); return M2_ECUDA; }
+    if (path == M2_PATH_SMALL) {
+        raw->threads = m2k::small_threads_for((unsigned)h);
+        if (o.wg >= 32 && o.wg <= 256 && (o.wg & (o.wg - 1)) == 0) raw->threads = (int)o.wg;
+        raw->carry_threads = small_carry_threads(raw->L, raw->span, raw->threads);
+        if ((rc = dalloc(raw, &raw->d_test, sizeof(m2k::SmallTest)))) { m2_destroy(c.release()); return rc; }
+        m2k::SmallTest t{};
+        t.digits = raw->d_digits; t.w61 = raw->d_w61; t.w31 = raw->d_w31;
+        t.tw4 = raw->tw.tw4; t.tc = raw->tw.tc; t.status = raw->d_status;
+        t.p = p; t.iters = 0; t.ln = raw->L.ln; t.mode = mode; t.span = raw->span;
+        t.carry_threads = raw->carry_threads;
+        if (cudaMemcpy(raw->d_test, &t, sizeof(t), cudaMemcpyHostToDevice) != cudaSuccess) { m2_destroy(c.release()); return M2_ECUDA; }
+    } else {
+        const m2k::LargePlan& P = raw->plan;
+        raw->plan.mode = mode;
+        if ((rc = dalloc(raw, &raw->d_carries, sizeof(i64) * (size_t)P.R * P.G)) ||
+            (rc = dalloc(raw, &raw->d_za, sizeof(ulonglong2) * h)) || (rc = dalloc(raw, &raw->d_zb, sizeof(uint2) * h))) {
+            m2_destroy(c.release());
+            return rc;
+        }
+        raw->bufs = m2k::LargeBufs{raw->d_digits, raw->d_carries, raw->d_za, raw->d_zb, raw->d_w61, raw->d_w31,
+                                   raw->tw.tw4, raw->tw.tc, raw->d_status};
+        if (m2k::large_setup(P) != cudaSuccess) { m2_destroy(c.release()); return M2_EUNSUPPORTED; }
+    }
+    raw->bytes += raw->tw.bytes;
+    if ((rc = upload_state(raw, m2::digits_of_small(raw->L, mode == M2_MODE_LL ? 4 : 3)))) { m2_destroy(c.release()); return rc; }
+    *out = c.release();
+    return M2_OK;
+}
+
+int m2_iterate(m2_ctx* c, uint32_t k) {
+    if (!c) return M2_EINVAL;
+    if (k == 0) return M2_OK;
+    if (cudaSetDevice(c->device) != cudaSuccess) return M2_ECUDA;
+    cudaError_t e = cudaSuccess;
+    if (c->path == M2_PATH_SMALL) {
+        e = m2k::launch_small(c->d_test, 1, (unsigned)c->L.h, c->threads, k, c->stream);
+    } else {
+        for (uint32_t i = 0; i < k && e == cudaSuccess; ++i) e = m2k::launch_large_iteration(c->plan, c->bufs, c->stream);
+    }
+    if (e != cudaSuccess) return M2_ECUDA;
+    c->iteration += k;
+    return M2_OK;
+}
+
+int m2_sync(m2_ctx* c) {
+    if (!c) return M2_EINVAL;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return M2_ECUDA;
+    int st = 0;
+    if (cudaMemcpy(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return M2_ECUDA;
+    return st ? M2_ESTATE : M2_OK;
+}
+
+int m2_get_digits(m2_ctx* c, uint64_t* out) {
+    if (!c || !out) return M2_EINVAL;
+    std::vector<u64> canon;
+    int rc = read_canonical(c, canon);
+    if (rc) return rc;
+    std::memcpy(out, canon.data(), canon.size() * sizeof(u64));
+    return M2_OK;
+}
+
+int m2_set_digits(m2_ctx* c, const uint64_t* digits, uint32_t iteration) {
+    if (!c || !digits) return M2_EINVAL;
+    if (m2_sync(c) == M2_ECUDA) return M2_ECUDA;
+    std::vector<u64> canon;
+    try {
+        canon = m2::canonical_from_unsigned(c->L, digits);
+    } catch (const std::exception&) {
+        return M2_EINVAL;
+    }
+    int rc = upload_state(c, canon);
+    if (rc) return rc;
+    cudaMemset(c->d_status, 0, sizeof(int));
+    c->iteration = iteration;
+    return M2_OK;
+}
+
+int m2_res64(m2_ctx* c, uint64_t* out) {
+    if (!c || !out) return M2_EINVAL;
+    std::vector<u64> canon;
+    int rc = read_canonical(c, canon);
+    if (rc) return rc;
+    *out = m2::res64_of(c->L, canon);
+    return M2_OK;
+}
+
+int m2_verdict(m2_ctx* c, int* is_prime) {
+    if (!c || !is_prime) return M2_EINVAL;
+    std::vector<u64> canon;
+    int rc = read_canonical(c, canon);
+    if (rc) return rc;
+    const u64 want = c->mode == M2_MODE_LL ? 0 : (c->mode == M2_MODE_PRP ? 9 : 3);
+    *is_prime = m2::equals_small(c->L, canon, want) ? 1 : 0;
+    return M2_OK;
+}
+
+int m2_info(m2_ctx* c, m2_info_t* info) {
+    if (!c || !info) return M2_EINVAL;
+    std::memset(info, 0, sizeof(*info));
+    info->p = c->L.p; info->mode = c->mode; info->ln = c->L.ln; info->n = c->L.n;
+    info->iteration = c->iteration;
+    info->total_iters = total_iters_for(c->L.p, c->mode);
+    info->path = c->path;
+    info->span = (uint32_t)c->span;
+    if (c->path == M2_PATH_LARGE) { info->rows = c->plan.R; info->row_len = c->plan.B; info->cols_per_cta = c->plan.C; }
+    else { info->rows = 1; info->row_len = (uint32_t)c->L.h; info->cols_per_cta = (uint32_t)c->threads; }
+    info->device_bytes = c->bytes;
+    return M2_OK;
+}
+
+void m2_destroy(m2_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->d_w61); cudaFree(c->d_w31); cudaFree(c->d_status); cudaFree(c->d_digits);
+    cudaFree(c->d_test); cudaFree(c->d_carries); cudaFree(c->d_za); cudaFree(c->d_zb);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+// ---------------- batched engine ----------------
+// Tests are bucketed by transform length h; every bucket is one persistent
+// launch (CTAs pull test indices from a device counter, longest tests first),
+// all buckets run concurrently on their own streams, and the whole set of
+// launches is captured into one CUDA graph.
+int m2_batch_run(const uint32_t* p, const int* modes, const uint32_t* iters, size_t count,
+                 uint64_t* res64_out, int* is_prime_out, int device, m2_batch_stats* stats) {
+    if (!p || count == 0) return M2_EINVAL;
+    if (cudaSetDevice(device) != cudaSuccess) { cudaGetLastError(); return M2_EINVAL; }
+    struct Item { size_t idx; m2::Layout L; int mode; u32 iters; int span; };
+    std::map<u64, std::vector<Item>> buckets;
+    for (size_t i = 0; i < count; ++i) {
+        const int mode = modes ? modes[i] : M2_MODE_PRP;
+        if (p[i] < 3 || mode < M2_MODE_LL || mode > M2_MODE_PRP3) return M2_EINVAL;
+        if (m2::transform_log2(p[i]) > 14) return M2_EUNSUPPORTED;   // h <= 8192
+        Item it;
+        it.idx = i; it.L = m2::make_layout(p[i]); it.mode = mode;
+        it.iters = iters ? iters[i] : total_iters_for(p[i], mode);
+        it.span = m2::carry_span(it.L);
+        buckets[it.L.h].push_back(std::move(it));
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    struct Dev {
+        std::vector<void*> allocs;
+        std::vector<cudaStream_t> streams;
+        std::vector<cudaEvent_t> events;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        ~Dev() {
+            if (exec) cudaGraphExecDestroy(exec);
+            if (graph) cudaGraphDestroy(graph);
+            for (auto e : events) cudaEventDestroy(e);
+            for (auto s : streams) cudaStreamDestroy(s);
+            for (auto a : allocs) cudaFree(a);
+        }
+    } dv;
+    auto dmal = [&](void** ptr, size_t bytes) -> int {
+        if (cudaMalloc(ptr, bytes) != cudaSuccess) { cudaGetLastError(); return M2_ENOMEM; }
+        dv.allocs.push_back(*ptr);
+        return M2_OK;
+    };
+    struct Launch { u64 h; int threads; int ntests; int grid; m2k::SmallTest* d_tests; int* d_queue; long long* d_dig; std::vector<Item>* items; };
+    std::vector<Launch> launches;
+    uint64_t squarings = 0;
+    for (auto& kv : buckets) {
+        const u64 h = kv.first;
+        std::vector<Item>& items = kv.second;
+        std::sort(items.begin(), items.end(), [](const Item& a, const Item& b) { return a.iters > b.iters; });
+        const u64 n = 2 * h;
+        const size_t nt = items.size();
+        TwTables tw;
+        int rc = get_twiddles(device, h, tw);
+        if (rc) return rc;
+        long long* d_dig = nullptr; unsigned char* d_w = nullptr; m2k::SmallTest* d_tests = nullptr; int* d_q = nullptr;
+        if ((rc = dmal((void**)&d_dig, nt * n * sizeof(i64))) || (rc = dmal((void**)&d_w, nt * n * 2)) ||
+            (rc = dmal((void**)&d_tests, nt * sizeof(m2k::SmallTest))) || (rc = dmal((void**)&d_q, 2 * sizeof(int))))
+            return rc;
+        const int threads = m2k::small_threads_for((unsigned)h);
+        std::vector<i64> dig(nt * n);
+        std::vector<unsigned char> w(nt * n * 2);
+        std::vector<m2k::SmallTest> tests(nt);
+        for (size_t t = 0; t < nt; ++t) {
+            const Item& it = items[t];
+            std::vector<i64> b = m2::balanced_digits(it.L, m2::digits_of_small(it.L, it.mode == M2_MODE_LL ? 4 : 3));
+            std::copy(b.begin(), b.end(), dig.begin() + t * n);
+            std::copy(it.L.w61.begin(), it.L.w61.end(), w.begin() + t * 2 * n);
+            std::copy(it.L.w31.begin(), it.L.w31.end(), w.begin() + t * 2 * n + n);
+            m2k::SmallTest& T = tests[t];
+            T.digits = d_dig + t * n; T.w61 = d_w + t * 2 * n; T.w31 = d_w + t * 2 * n + n;
+            T.tw4 = tw.tw4; T.tc = tw.tc; T.status = d_q + 1;
+            T.p = it.L.p; T.iters = it.iters; T.ln = it.L.ln; T.mode = it.mode; T.span = it.span;
+            T.carry_threads = small_carry_threads(it.L, it.span, threads);
+            squarings += it.iters;
+        }
+        if (cudaMemcpy(d_dig, dig.data(), dig.size() * sizeof(i64), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(d_w, w.data(), w.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(d_tests, tests.data(), tests.size() * sizeof(m2k::SmallTest), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemset(d_q, 0, 2 * sizeof(int)) != cudaSuccess)
+            return M2_ECUDA;
+        const int per_sm = m2k::small_ctas_per_sm((unsigned)h, threads);
+        const int grid = (int)std::min<size_t>(nt, (size_t)per_sm * (size_t)std::max(sms, 1));
+        launches.push_back(Launch{h, threads, (int)nt, grid, d_tests, d_q, d_dig, &items});
+    }
+    // capture: fork from stream 0 to one stream per bucket, join back
+    dv.streams.resize(launches.size() + 1);
+    for (auto& s : dv.streams) if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return M2_ECUDA;
+    dv.events.resize(launches.size() + 3);
+    for (auto& e : dv.events) if (cudaEventCreate(&e) != cudaSuccess) return M2_ECUDA;
+    cudaStream_t s0 = dv.streams[0];
+    if (cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return M2_ECUDA;
+    cudaEventRecord(dv.events[0], s0);
+    for (size_t b = 0; b < launches.size(); ++b) {
+        cudaStream_t sb = dv.streams[b + 1];
+        cudaStreamWaitEvent(sb, dv.events[0], 0);
+        const Launch& l = launches[b];
+        m2k::launch_small_persistent(l.d_tests, l.ntests, (unsigned)l.h, l.threads, l.d_queue, l.grid, sb);
+        cudaEventRecord(dv.events[b + 3], sb);
+        cudaStreamWaitEvent(s0, dv.events[b + 3], 0);
+    }
+    if (cudaStreamEndCapture(s0, &dv.graph) != cudaSuccess) return M2_ECUDA;
+    if (cudaGraphInstantiate(&dv.exec, dv.graph, 0) != cudaSuccess) return M2_ECUDA;
+    cudaEvent_t t0 = dv.events[1], t1 = dv.events[2];
+    cudaEventRecord(t0, s0);
+    if (cudaGraphLaunch(dv.exec, s0) != cudaSuccess) return M2_ECUDA;
+    cudaEventRecord(t1, s0);
+    if (cudaStreamSynchronize(s0) != cudaSuccess) return M2_ECUDA;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, t0, t1);
+    int status_any = 0;
+    for (const Launch& l : launches) {
+        int st = 0;
+        if (cudaMemcpy(&st, l.d_queue + 1, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return M2_ECUDA;
+        status_any |= st;
+        const u64 n = 2 * l.h;
+        std::vector<i64> dig((size_t)l.ntests * n);
+        if (cudaMemcpy(dig.data(), l.d_dig, dig.size() * sizeof(i64), cudaMemcpyDeviceToHost) != cudaSuccess) return M2_ECUDA;
+        for (int t = 0; t < l.ntests; ++t) {
+            const Item& it = (*l.items)[t];
+            std::vector<i64> d(dig.begin() + (size_t)t * n, dig.begin() + (size_t)(t + 1) * n);
+            std::vector<u64> canon;
+            try { canon = m2::canonical_digits(it.L, d, {}, 0); } catch (const std::exception&) { return M2_ESTATE; }
+            if (res64_out) res64_out[it.idx] = m2::res64_of(it.L, canon);
+            if (is_prime_out) {
+                const u64 want = it.mode == M2_MODE_LL ? 0 : (it.mode == M2_MODE_PRP ? 9 : 3);
+                is_prime_out[it.idx] = m2::equals_small(it.L, canon, want) ? 1 : 0;
+            }
+        }
+    }
+    if (stats) {
+        stats->seconds = ms * 1e-3;
+        stats->squarings = squarings;
+        stats->launches = (uint32_t)launches.size();
+        stats->buckets = (uint32_t)buckets.size();
+    }
+    return status_any ? M2_ESTATE : M2_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,508 @@
+// m2_kernels.cu -- sm_103a kernels of the squaring chain x <- x^2 (-2) mod 2^p - 1.
+//
+// State between iterations: n balanced signed digits d_j (|d_j| <~ 2^(w_j-1),
+// widths w_j = ceil(p(j+1)/n) - ceil(pj/n)), in natural order, as int64.
+// One squaring is an IBDWT over GF(P61^2) x GF(P31^2):
+//   weight (rotate by the IBDWT shift) -> forward transform (in-place DIF with
+//   per-block twiddles, natural in, bit-reversed out) -> real-packed centre
+//   square -> inverse transform -> unweight (includes the 1/(2n) scale) ->
+//   Garner CRT to a signed 92-bit word -> balanced carry.
+//
+// Two execution shapes:
+//  * k_small: one CTA owns one whole test (state in shared memory) and loops
+//    over iterations on-chip.  Used for n <= 16384 and by the batched engine
+//    (one CTA per test, many tests per launch).
+//  * three-pass path for large n, h = R x B elements:
+//      k_cols_fwd: apply pending segment carries, weight, first log2 R levels
+//                  down the columns (C adjacent columns per CTA)
+//      k_rows:     last log2 B levels, centre square, first inverse levels on a
+//                  pair of mirror rows per CTA
+//      k_cols_inv: last inverse levels on the columns, unweight, CRT, carry
+//                  within each row segment of C elements; the segment's carry
+//                  out is applied by the next k_cols_fwd.
+#include "m2_kernels.cuh"
+#include "m2_field.cuh"
+
+using namespace m2d;
+
+namespace m2k {
+
+namespace {
+
+struct SE {
+    u64* a; u64* b; u32* c; u32* d;
+    __device__ __forceinline__ E ld(u32 i) const { return E{a[i], b[i], c[i], d[i]}; }
+    __device__ __forceinline__ void st(u32 i, const E& e) const { a[i] = e.a; b[i] = e.b; c[i] = e.c; d[i] = e.d; }
+};
+__device__ __forceinline__ SE make_se(unsigned char* base, u32 ne) {
+    return SE{(u64*)base, (u64*)base + ne, (u32*)(base + 16ull * ne), (u32*)(base + 16ull * ne) + ne};
+}
+
+__device__ __forceinline__ E ldtw(const DTw* t, u32 i) {
+    const u64* q = reinterpret_cast<const u64*>(t + i);
+    const u64 a = __ldg(q), b = __ldg(q + 1), cd = __ldg(q + 2);
+    return E{a, b, (u32)cd, (u32)(cd >> 32)};
+}
+
+__device__ __forceinline__ u64 bitpos(u32 p, int ln, u64 j) { return j ? ((((u64)p * j) - 1) >> ln) + 1 : 0; }
+__device__ __forceinline__ u32 width_of(u32 p, int ln, u64 j) { return (u32)(bitpos(p, ln, j + 1) - bitpos(p, ln, j)); }
+
+__device__ __forceinline__ E weigh(i64 d0, i64 d1, u32 s061, u32 s161, u32 s031, u32 s131) {
+    return E{rotl61(digit_to61(d0), s061), rotl61(digit_to61(d1), s161), rotl31(digit_to31(d0), s031), rotl31(digit_to31(d1), s131)};
+}
+// multiplier 2^-(s + ln + 1) as a left rotation
+__device__ __forceinline__ u32 unrot61(u32 s, int ln) { const u32 t = (s + (u32)ln + 1u) % 61u; return t ? 61u - t : 0u; }
+__device__ __forceinline__ u32 unrot31(u32 s, int ln) { const u32 t = (s + (u32)ln + 1u) % 31u; return t ? 31u - t : 0u; }
+
+// unweight element k (digits 2k, 2k+1) and return the two signed convolution words
+__device__ __forceinline__ void unweigh_crt(const E& v, u64 j, const unsigned char* w61, const unsigned char* w31, int ln,
+                                            int mode, i128& z0, i128& z1) {
+    const u64 a = rotl61(v.a, unrot61(w61[j], ln)), b = rotl61(v.b, unrot61(w61[j + 1], ln));
+    const u32 c = rotl31(v.c, unrot31(w31[j], ln)), d = rotl31(v.d, unrot31(w31[j + 1], ln));
+    z0 = crt_signed(a, c);
+    z1 = crt_signed(b, d);
+    if (mode == PRP3) { z0 *= 3; z1 *= 3; }
+}
+
+__device__ __forceinline__ bool fits64(i128 c) { const i128 hi = c >> 63; return hi == 0 || hi == -1; }
+
+}  // namespace
+
+// =====================================================================
+// k_small: whole test in one CTA
+// =====================================================================
+__device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, unsigned char* smem) {
+    const SE z = make_se(smem, h);
+    i64* cx = reinterpret_cast<i64*>(smem + 24ull * h);
+    const u32 tid = threadIdx.x, nt = blockDim.x;
+    const u64 n = 2ull * h;
+    const int ln = T.ln;
+    const u32 p = T.p;
+    const int L = ln - 1;
+    const bool odd = (L & 1) != 0;
+    u32 s4max = 0;
+    for (u32 S = 1; 4 * S <= h; S *= 4) s4max = S;
+
+    for (u32 k = tid; k < h; k += nt) { z.a[k] = (u64)T.digits[2 * k]; z.b[k] = (u64)T.digits[2 * k + 1]; }
+    __syncthreads();
+
+    for (u32 it = 0; it < iters; ++it) {
+        for (u32 k = tid; k < h; k += nt) {
+            const i64 d0 = (i64)z.a[k], d1 = (i64)z.b[k];
+            z.st(k, weigh(d0, d1, T.w61[2 * k], T.w61[2 * k + 1], T.w31[2 * k], T.w31[2 * k + 1]));
+        }
+        __syncthreads();
+        // forward radix-4 steps, S blocks of M = h/S
+        for (u32 S = 1; S <= s4max && s4max; S *= 4) {
+            const u32 M = h / S, Q = M >> 2;
+            for (u32 b = tid; b < h / 4; b += nt) {
+                const u32 j = b / Q, i = b % Q, base = j * M + i;
+                E x0 = z.ld(base), x1 = z.ld(base + Q), x2 = z.ld(base + 2 * Q), x3 = z.ld(base + 3 * Q);
+                const u32 ti = 3 * (S + j);
+                dif4(x0, x1, x2, x3, ldtw(T.tw4, ti), ldtw(T.tw4, ti + 1), ldtw(T.tw4, ti + 2));
+                z.st(base, x0); z.st(base + Q, x1); z.st(base + 2 * Q, x2); z.st(base + 3 * Q, x3);
+            }
+            __syncthreads();
+        }
+        if (odd) {
+            for (u32 b = tid; b < h / 2; b += nt) {
+                E x0 = z.ld(2 * b), x1 = z.ld(2 * b + 1);
+                dif2(x0, x1, ldtw(T.tc, b));
+                z.st(2 * b, x0); z.st(2 * b + 1, x1);
+            }
+            __syncthreads();
+        }
+        // centre: even position k with its mirror 3*2^e - k - 1
+        for (u32 b = tid; b < h / 2; b += nt) {
+            const u32 k = 2 * b;
+            if (k == 0) {
+                E z0 = z.ld(0), z1 = z.ld(1);
+                centre_zero(z0, z1);
+                z.st(0, z0); z.st(1, z1);
+            } else {
+                const u32 e = 31u - __clz(k);
+                const u32 mk = (3u << e) - k - 1u;
+                E zk = z.ld(k), zm = z.ld(mk);
+                centre_pair(zk, zm, ldtw(T.tc, b));
+                z.st(k, zk); z.st(mk, zm);
+            }
+        }
+        __syncthreads();
+        if (odd) {
+            for (u32 b = tid; b < h / 2; b += nt) {
+                E x0 = z.ld(2 * b), x1 = z.ld(2 * b + 1);
+                dit2(x0, x1, ldtw(T.tc, b));
+                z.st(2 * b, x0); z.st(2 * b + 1, x1);
+            }
+            __syncthreads();
+        }
+        for (u32 S = s4max; S >= 1 && s4max; S /= 4) {
+            const u32 M = h / S, Q = M >> 2;
+            for (u32 b = tid; b < h / 4; b += nt) {
+                const u32 j = b / Q, i = b % Q, base = j * M + i;
+                E x0 = z.ld(base), x1 = z.ld(base + Q), x2 = z.ld(base + 2 * Q), x3 = z.ld(base + 3 * Q);
+                const u32 ti = 3 * (S + j);
+                dit4(x0, x1, x2, x3, ldtw(T.tw4, ti), ldtw(T.tw4, ti + 1), ldtw(T.tw4, ti + 2));
+                z.st(base, x0); z.st(base + Q, x1); z.st(base + 2 * Q, x2); z.st(base + 3 * Q, x3);
+            }
+            __syncthreads();
+            if (S == 1) break;
+        }
+        // unweight, CRT, carry
+        const int Tc = T.carry_threads;
+        if (Tc == 0) {
+            // tiny exponents: one thread, full normalization with wrap-around
+            if (tid == 0) {
+                i128 c = 0;
+                for (u32 k = 0; k < h; ++k) {
+                    i128 z0, z1;
+                    unweigh_crt(z.ld(k), 2ull * k, T.w61, T.w31, ln, T.mode, z0, z1);
+                    if (T.mode == LL && k == 0) z0 -= 2;
+                    const i64 d0 = split_balanced(z0 + c, width_of(p, ln, 2ull * k), c);
+                    const i64 d1 = split_balanced(z1 + c, width_of(p, ln, 2ull * k + 1), c);
+                    z.a[k] = (u64)d0; z.b[k] = (u64)d1;
+                }
+                int pass = 0;
+                while (c != 0 && pass < 8) {
+                    for (u64 j = 0; j < n && c != 0; ++j) {
+                        u64* slot = (j & 1) ? &z.b[j >> 1] : &z.a[j >> 1];
+                        *slot = (u64)split_balanced((i128)(i64)*slot + c, width_of(p, ln, j), c);
+                    }
+                    ++pass;
+                }
+                if (c != 0) atomicExch(T.status, ST_NORMALIZE);
+            }
+            __syncthreads();
+        } else {
+            const u32 D = (u32)(n / (u64)Tc);
+            if (tid < (u32)Tc) {
+                i128 c = 0;
+                const u64 j0 = (u64)tid * D;
+                for (u32 u = 0; u < D; u += 2) {
+                    const u32 k = (u32)((j0 + u) >> 1);
+                    i128 z0, z1;
+                    unweigh_crt(z.ld(k), 2ull * k, T.w61, T.w31, ln, T.mode, z0, z1);
+                    if (T.mode == LL && k == 0) z0 -= 2;
+                    const i64 d0 = split_balanced(z0 + c, width_of(p, ln, 2ull * k), c);
+                    const i64 d1 = split_balanced(z1 + c, width_of(p, ln, 2ull * k + 1), c);
+                    z.a[k] = (u64)d0; z.b[k] = (u64)d1;
+                }
+                if (!fits64(c)) atomicExch(T.status, ST_CARRY_RANGE);
+                cx[tid] = (i64)c;
+            }
+            __syncthreads();
+            if (tid < (u32)Tc) {
+                i64 c = cx[(tid + (u32)Tc - 1u) % (u32)Tc];
+                const u64 j0 = (u64)tid * D;
+                for (int u = 0; u <= T.span; ++u) {
+                    const u64 j = j0 + (u64)u;
+                    u64* slot = (j & 1) ? &z.b[j >> 1] : &z.a[j >> 1];
+                    if (u < T.span) *slot = (u64)split_balanced64((i64)*slot + c, width_of(p, ln, j), c);
+                    else *slot = (u64)((i64)*slot + c);
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (u32 k = tid; k < h; k += nt) { T.digits[2 * k] = (i64)z.a[k]; T.digits[2 * k + 1] = (i64)z.b[k]; }
+}
+
+// One CTA per test (queue == nullptr), or a persistent grid whose CTAs take
+// test indices from *queue until all `ntests` are done.
+__global__ void __launch_bounds__(256, 2) k_small(const SmallTest* tests, int ntests, u32 h, u32 iters_override, int* queue) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_next;
+    if (queue == nullptr) {
+        const SmallTest T = tests[blockIdx.x];
+        run_small(T, h, iters_override ? iters_override : T.iters, smem);
+        return;
+    }
+    for (;;) {
+        if (threadIdx.x == 0) s_next = atomicAdd(queue, 1);
+        __syncthreads();
+        const int idx = s_next;
+        __syncthreads();
+        if (idx >= ntests) break;
+        const SmallTest T = tests[idx];
+        run_small(T, h, iters_override ? iters_override : T.iters, smem);
+        __syncthreads();
+    }
+}
+
+int small_threads_for(unsigned int h) {
+    unsigned int t = h / 4;
+    if (t < 32) t = 32;
+    if (t > 256) t = 256;
+    return (int)t;
+}
+size_t small_smem_bytes(unsigned int h, int threads) { return 24ull * h + 8ull * (size_t)threads; }
+
+cudaError_t launch_small(const SmallTest* d_tests, int ntests, unsigned int h, int threads, unsigned int iters_override, cudaStream_t s) {
+    const size_t sm = small_smem_bytes(h, threads);
+    cudaError_t e = cudaFuncSetAttribute(k_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_small<<<ntests, threads, sm, s>>>(d_tests, ntests, h, iters_override, nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_small_persistent(const SmallTest* d_tests, int ntests, unsigned int h, int threads, int* d_queue,
+                                    int grid, cudaStream_t s) {
+    const size_t sm = small_smem_bytes(h, threads);
+    cudaError_t e = cudaFuncSetAttribute(k_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_small<<<grid, threads, sm, s>>>(d_tests, ntests, h, 0u, d_queue);
+    return cudaGetLastError();
+}
+
+int small_ctas_per_sm(unsigned int h, int threads) {
+    int nb = 0;
+    const size_t sm = small_smem_bytes(h, threads);
+    if (cudaFuncSetAttribute(k_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_small, threads, sm) != cudaSuccess) return 1;
+    return nb > 0 ? nb : 1;
+}
+
+// =====================================================================
+// three-pass path
+// =====================================================================
+constexpr int LT = 256;   // threads per CTA of the large-path kernels
+
+template <int C>
+__global__ void __launch_bounds__(LT) k_cols_fwd(LargePlan P, LargeBufs bf) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const u32 R = P.R, B = P.B, G = P.G, g = blockIdx.x;
+    const u32 NE = (u32)C * R;
+    const SE z = make_se(smem, NE);
+    const u64 RG = (u64)R * G;
+    const u32 p = P.p;
+    const int ln = P.ln;
+    for (u32 t = threadIdx.x; t < R; t += blockDim.x) {
+        const u64 s = (u64)t * G + g;
+        i64 c = bf.carries[(s + RG - 1) % RG];
+        const u64 e0 = (u64)t * B + (u64)g * C;
+        const u64 j0 = 2 * e0;
+        i64 d[2 * C];
+#pragma unroll
+        for (int u = 0; u < 2 * C; ++u) d[u] = bf.digits[j0 + u];
+#pragma unroll
+        for (int u = 0; u < 2 * C; ++u) {
+            if (u < P.span) d[u] = split_balanced64(d[u] + c, width_of(p, ln, j0 + u), c);
+            else if (u == P.span) d[u] += c;
+        }
+#pragma unroll
+        for (int cc = 0; cc < C; ++cc) {
+            const u64 j = j0 + 2 * cc;
+            z.st(t * C + cc, weigh(d[2 * cc], d[2 * cc + 1], bf.w61[j], bf.w61[j + 1], bf.w31[j], bf.w31[j + 1]));
+        }
+    }
+    __syncthreads();
+    for (u32 S = 1; S < R; S *= 4) {
+        const u32 M = R / S, Q = M >> 2;
+        for (u32 b = threadIdx.x; b < NE / 4; b += blockDim.x) {
+            const u32 cc = b % C, rho = b / C, j = rho / Q, i = rho % Q;
+            const u32 r0 = j * M + i;
+            const u32 i0 = r0 * C + cc, i1 = (r0 + Q) * C + cc, i2 = (r0 + 2 * Q) * C + cc, i3 = (r0 + 3 * Q) * C + cc;
+            E x0 = z.ld(i0), x1 = z.ld(i1), x2 = z.ld(i2), x3 = z.ld(i3);
+            const u32 ti = 3 * (S + j);
+            dif4(x0, x1, x2, x3, ldtw(bf.tw4, ti), ldtw(bf.tw4, ti + 1), ldtw(bf.tw4, ti + 2));
+            z.st(i0, x0); z.st(i1, x1); z.st(i2, x2); z.st(i3, x3);
+        }
+        __syncthreads();
+    }
+    for (u32 l = threadIdx.x; l < NE; l += blockDim.x) {
+        const u32 t = l / C, cc = l % C;
+        const u64 e = (u64)t * B + (u64)g * C + cc;
+        const E v = z.ld(l);
+        bf.za[e] = make_ulonglong2(v.a, v.b);
+        bf.zb[e] = make_uint2(v.c, v.d);
+    }
+}
+
+__global__ void __launch_bounds__(LT) k_rows(LargePlan P, LargeBufs bf) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const u32 B = P.B, NE = 2 * B;
+    const SE z = make_se(smem, NE);
+    const u32 pi = blockIdx.x;
+    u32 t0, t1;
+    if (pi == 0) { t0 = 0; t1 = 1; }
+    else {
+        const u32 e = 32u - __clz(pi);                 // floor(log2 pi) + 1
+        const u32 a = pi - (1u << (e - 1));
+        t0 = (1u << e) + a;
+        t1 = (2u << e) - 1u - a;
+    }
+    for (u32 l = threadIdx.x; l < NE; l += blockDim.x) {
+        const u32 sl = l / B, col = l % B;
+        const u64 e = (u64)(sl ? t1 : t0) * B + col;
+        const ulonglong2 va = bf.za[e];
+        const uint2 vb = bf.zb[e];
+        z.st(l, E{va.x, va.y, vb.x, vb.y});
+    }
+    __syncthreads();
+    const u32 per4 = B / 4;
+    u32 S = P.R, Mloc = B;
+    for (; Mloc >= 4; S *= 4, Mloc /= 4) {
+        const u32 Q = Mloc >> 2, nb = B / Mloc;
+        for (u32 b = threadIdx.x; b < 2 * per4; b += blockDim.x) {
+            const u32 sl = b / per4, rho = b % per4, j = rho / Q, i = rho % Q;
+            const u32 base = sl * B + j * Mloc + i;
+            const u32 J = (sl ? t1 : t0) * nb + j;
+            E x0 = z.ld(base), x1 = z.ld(base + Q), x2 = z.ld(base + 2 * Q), x3 = z.ld(base + 3 * Q);
+            const u64 ti = 3ull * ((u64)S + J);
+            dif4(x0, x1, x2, x3, ldtw(bf.tw4, (u32)ti), ldtw(bf.tw4, (u32)ti + 1), ldtw(bf.tw4, (u32)ti + 2));
+            z.st(base, x0); z.st(base + Q, x1); z.st(base + 2 * Q, x2); z.st(base + 3 * Q, x3);
+        }
+        __syncthreads();
+    }
+    const bool odd = (Mloc == 2);
+    const u32 per2 = B / 2;
+    if (odd) {
+        for (u32 b = threadIdx.x; b < 2 * per2; b += blockDim.x) {
+            const u32 sl = b / per2, rho = b % per2, base = sl * B + 2 * rho;
+            const u32 J = (sl ? t1 : t0) * per2 + rho;
+            E x0 = z.ld(base), x1 = z.ld(base + 1);
+            dif2(x0, x1, ldtw(bf.tc, J));
+            z.st(base, x0); z.st(base + 1, x1);
+        }
+        __syncthreads();
+    }
+    // centre
+    for (u32 b = threadIdx.x; b < B; b += blockDim.x) {
+        const u32 sl = b / per2, i = 2 * (b % per2);
+        const u64 k = (u64)(sl ? t1 : t0) * B + i;
+        const u32 li = sl * B + i;
+        if (pi == 0) {
+            if (k == 0) {
+                E a0 = z.ld(0), a1 = z.ld(1);
+                centre_zero(a0, a1);
+                z.st(0, a0); z.st(1, a1);
+            } else {
+                const u32 e = 63u - (u32)__clzll((long long)k);
+                const u64 mk = (3ull << e) - k - 1ull;
+                const u32 lm = sl * B + (u32)(mk % B);
+                E zk = z.ld(li), zm = z.ld(lm);
+                centre_pair(zk, zm, ldtw(bf.tc, (u32)(k >> 1)));
+                z.st(li, zk); z.st(lm, zm);
+            }
+        } else {
+            const u32 lm = (1u - sl) * B + (B - 1u - i);
+            E zk = z.ld(li), zm = z.ld(lm);
+            centre_pair(zk, zm, ldtw(bf.tc, (u32)(k >> 1)));
+            z.st(li, zk); z.st(lm, zm);
+        }
+    }
+    __syncthreads();
+    if (odd) {
+        for (u32 b = threadIdx.x; b < 2 * per2; b += blockDim.x) {
+            const u32 sl = b / per2, rho = b % per2, base = sl * B + 2 * rho;
+            const u32 J = (sl ? t1 : t0) * per2 + rho;
+            E x0 = z.ld(base), x1 = z.ld(base + 1);
+            dit2(x0, x1, ldtw(bf.tc, J));
+            z.st(base, x0); z.st(base + 1, x1);
+        }
+        __syncthreads();
+    }
+    // inverse radix-4 steps in reverse order
+    for (S /= 4, Mloc = odd ? 8 : 4; Mloc <= B && S >= P.R; S /= 4, Mloc *= 4) {
+        const u32 Q = Mloc >> 2, nb = B / Mloc;
+        for (u32 b = threadIdx.x; b < 2 * per4; b += blockDim.x) {
+            const u32 sl = b / per4, rho = b % per4, j = rho / Q, i = rho % Q;
+            const u32 base = sl * B + j * Mloc + i;
+            const u32 J = (sl ? t1 : t0) * nb + j;
+            E x0 = z.ld(base), x1 = z.ld(base + Q), x2 = z.ld(base + 2 * Q), x3 = z.ld(base + 3 * Q);
+            const u64 ti = 3ull * ((u64)S + J);
+            dit4(x0, x1, x2, x3, ldtw(bf.tw4, (u32)ti), ldtw(bf.tw4, (u32)ti + 1), ldtw(bf.tw4, (u32)ti + 2));
+            z.st(base, x0); z.st(base + Q, x1); z.st(base + 2 * Q, x2); z.st(base + 3 * Q, x3);
+        }
+        __syncthreads();
+        if (S == P.R) break;
+    }
+    for (u32 l = threadIdx.x; l < NE; l += blockDim.x) {
+        const u32 sl = l / B, col = l % B;
+        const u64 e = (u64)(sl ? t1 : t0) * B + col;
+        const E v = z.ld(l);
+        bf.za[e] = make_ulonglong2(v.a, v.b);
+        bf.zb[e] = make_uint2(v.c, v.d);
+    }
+}
+
+template <int C>
+__global__ void __launch_bounds__(LT) k_cols_inv(LargePlan P, LargeBufs bf) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const u32 R = P.R, B = P.B, G = P.G, g = blockIdx.x;
+    const u32 NE = (u32)C * R;
+    const SE z = make_se(smem, NE);
+    const u32 p = P.p;
+    const int ln = P.ln;
+    for (u32 l = threadIdx.x; l < NE; l += blockDim.x) {
+        const u32 t = l / C, cc = l % C;
+        const u64 e = (u64)t * B + (u64)g * C + cc;
+        const ulonglong2 va = bf.za[e];
+        const uint2 vb = bf.zb[e];
+        z.st(l, E{va.x, va.y, vb.x, vb.y});
+    }
+    __syncthreads();
+    for (u32 S = R / 4; S >= 1; S /= 4) {
+        const u32 M = R / S, Q = M >> 2;
+        for (u32 b = threadIdx.x; b < NE / 4; b += blockDim.x) {
+            const u32 cc = b % C, rho = b / C, j = rho / Q, i = rho % Q;
+            const u32 r0 = j * M + i;
+            const u32 i0 = r0 * C + cc, i1 = (r0 + Q) * C + cc, i2 = (r0 + 2 * Q) * C + cc, i3 = (r0 + 3 * Q) * C + cc;
+            E x0 = z.ld(i0), x1 = z.ld(i1), x2 = z.ld(i2), x3 = z.ld(i3);
+            const u32 ti = 3 * (S + j);
+            dit4(x0, x1, x2, x3, ldtw(bf.tw4, ti), ldtw(bf.tw4, ti + 1), ldtw(bf.tw4, ti + 2));
+            z.st(i0, x0); z.st(i1, x1); z.st(i2, x2); z.st(i3, x3);
+        }
+        __syncthreads();
+        if (S == 1) break;
+    }
+    for (u32 t = threadIdx.x; t < R; t += blockDim.x) {
+        const u64 e0 = (u64)t * B + (u64)g * C;
+        i128 c = 0;
+#pragma unroll
+        for (int cc = 0; cc < C; ++cc) {
+            const u64 e = e0 + cc, j = 2 * e;
+            i128 z0, z1;
+            unweigh_crt(z.ld(t * C + cc), j, bf.w61, bf.w31, ln, P.mode, z0, z1);
+            if (P.mode == LL && e == 0) z0 -= 2;
+            const i64 d0 = split_balanced(z0 + c, width_of(p, ln, j), c);
+            const i64 d1 = split_balanced(z1 + c, width_of(p, ln, j + 1), c);
+            bf.digits[j] = d0;
+            bf.digits[j + 1] = d1;
+        }
+        if (!fits64(c)) atomicExch(bf.status, ST_CARRY_RANGE);
+        bf.carries[(u64)t * G + g] = (i64)c;
+    }
+}
+
+size_t large_smem_cols(const LargePlan& P) { return 24ull * P.C * P.R; }
+size_t large_smem_rows(const LargePlan& P) { return 24ull * 2 * P.B; }
+
+#define M2_FOR_C(X) X(4) X(8) X(16)
+
+cudaError_t large_setup(const LargePlan& P) {
+    cudaError_t e;
+    const int sc = (int)large_smem_cols(P), sr = (int)large_smem_rows(P);
+#define M2_SET(CC)                                                                                          \
+    if (P.C == CC) {                                                                                        \
+        if ((e = cudaFuncSetAttribute(k_cols_fwd<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, sc))) return e; \
+        if ((e = cudaFuncSetAttribute(k_cols_inv<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, sc))) return e; \
+    }
+    M2_FOR_C(M2_SET)
+#undef M2_SET
+    return cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, sr);
+}
+
+cudaError_t launch_large_iteration(const LargePlan& P, const LargeBufs& b, cudaStream_t s) {
+    const size_t sc = large_smem_cols(P), sr = large_smem_rows(P);
+#define M2_FWD(CC) if (P.C == CC) k_cols_fwd<CC><<<P.G, LT, sc, s>>>(P, b);
+    M2_FOR_C(M2_FWD)
+#undef M2_FWD
+    k_rows<<<P.R / 2, LT, sr, s>>>(P, b);
+#define M2_INV(CC) if (P.C == CC) k_cols_inv<CC><<<P.G, LT, sc, s>>>(P, b);
+    M2_FOR_C(M2_INV)
+#undef M2_INV
+    return cudaGetLastError();
+}
+
+}  // namespace m2k

@@ -1,0 +1,67 @@
+// m2_kernels.cuh -- kernel parameter blocks and launch wrappers (host-visible).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace m2k {
+
+// Dual-field twiddle as stored on the device (24 bytes, same as m2::Dual).
+struct DTw { unsigned long long a, b; unsigned int c, d; };
+
+enum Mode : int { LL = 0, PRP = 1, PRP3 = 2 };
+
+// Status word written by kernels (0 = ok).
+enum Status : int { ST_OK = 0, ST_CARRY_RANGE = 1, ST_NORMALIZE = 2 };
+
+// One independent test for the whole-iteration-in-one-CTA kernel.
+struct SmallTest {
+    long long* digits;        // n balanced digits (in/out)
+    const unsigned char* w61; // n shifts
+    const unsigned char* w31;
+    const DTw* tw4;           // radix-4 twiddles of this h
+    const DTw* tc;            // centre twiddles of this h
+    int* status;
+    unsigned int p;
+    unsigned int iters;
+    int ln;
+    int mode;
+    int span;                 // carry span (digits normalized after a segment carry)
+    int carry_threads;        // threads taking part in the segmented carry (0 = one thread, full normalization)
+};
+
+// Plan of the three-pass path for one transform length.
+struct LargePlan {
+    int ln, L, L1, L2;        // log2 n, log2 h, log2 rows, log2 row length
+    unsigned int R, B, C, G;  // rows, row length, columns per CTA, column groups
+    int span;
+    unsigned int p;
+    int mode;
+};
+
+struct LargeBufs {
+    long long* digits;        // n
+    long long* carries;       // R*G segment carries
+    ulonglong2* za;           // h GF(P61^2) coordinates
+    uint2* zb;                // h GF(P31^2) coordinates
+    const unsigned char* w61;
+    const unsigned char* w31;
+    const DTw* tw4;
+    const DTw* tc;
+    int* status;
+};
+
+size_t small_smem_bytes(unsigned int h, int threads);
+int small_threads_for(unsigned int h);
+// iters_override != 0 replaces every test's iteration count for this launch
+cudaError_t launch_small(const SmallTest* d_tests, int ntests, unsigned int h, int threads, unsigned int iters_override, cudaStream_t s);
+// persistent grid: CTAs take test indices from *d_queue (zeroed by the caller)
+cudaError_t launch_small_persistent(const SmallTest* d_tests, int ntests, unsigned int h, int threads, int* d_queue,
+                                    int grid, cudaStream_t s);
+int small_ctas_per_sm(unsigned int h, int threads);
+
+size_t large_smem_cols(const LargePlan& P);
+size_t large_smem_rows(const LargePlan& P);
+cudaError_t large_setup(const LargePlan& P);   // sets max dynamic smem attributes
+cudaError_t launch_large_iteration(const LargePlan& P, const LargeBufs& b, cudaStream_t s);
+
+}  // namespace m2k

@@ -1,0 +1,82 @@
+"""Parity of the CUDA engine against the CPU oracle, through the C ABI.
+
+Bit-exact: the canonical digit vector (the reference's state after its carry,
+mersenne2_gpu.cpp:2116) must equal the oracle's at every compared iteration.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TINY = [3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61, 67, 89, 107, 127]
+
+
+def _cmp(got, want, what):
+    if not np.array_equal(got, want):
+        bad = np.nonzero(got != want)[0]
+        raise AssertionError(f"{what}: {len(bad)} digits differ, first at {bad[0]}: {got[bad[0]]} != {want[bad[0]]}")
+
+
+@pytest.mark.parametrize("p", TINY)
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_tiny_exponents_full_run(m2, oracle_mod, p, mode):
+    """Tiny p (zero-width digits for p < 8): full runs against exact integers."""
+    with m2.Engine(p, mode) as e:
+        iters = m2.total_iterations(p, mode)
+        e.iterate(iters)
+        want = oracle_mod.python_chain(p, mode, iters) % ((1 << p) - 1)
+        assert e.res64() == want & ((1 << 64) - 1)
+        _, _, w = m2.layout(p)
+        _cmp(e.digits(), oracle_mod.digits_of_value(want, w), f"p={p} mode={mode}")
+        assert e.verdict() == (want == {0: 0, 1: 9 % ((1 << p) - 1), 2: 3 % ((1 << p) - 1)}[mode])
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_9941_state_every_1000(m2, oracle_mod, mode):
+    """Config 1: p = 9941 (n = 256), full run, full state every 1000 iterations."""
+    p = 9941
+    o = oracle_mod.Oracle(p, mode)
+    total = m2.total_iterations(p, mode)
+    with m2.Engine(p, mode) as e:
+        done = 0
+        while done < total:
+            k = min(1000, total - done)
+            e.iterate(k)
+            o.iterate(k)
+            done += k
+            _cmp(e.digits(), o.digits(), f"p=9941 mode={mode} iter={done}")
+        assert e.verdict()   # M_9941 is prime
+
+
+@pytest.mark.parametrize("p", [521, 1279, 2203, 4423, 9689, 21701, 44497, 86243, 132049, 216091])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_small_path_vs_oracle(m2, oracle_mod, p, mode):
+    iters = 200 if p < 100000 else 60
+    with m2.Engine(p, mode, path=m2.PATH_SMALL) as e:
+        e.iterate(iters)
+        got = e.digits()
+    o = oracle_mod.Oracle(p, mode)
+    o.iterate(iters)
+    _cmp(got, o.digits(), f"small p={p} mode={mode}")
+
+
+@pytest.mark.parametrize("p", [4423, 9941, 44497, 132049, 216091, 756839, 1398269, 2976221])
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_large_path_vs_oracle(m2, oracle_mod, p, mode):
+    iters = 40 if p < 1000000 else 6
+    with m2.Engine(p, mode, path=m2.PATH_LARGE) as e:
+        e.iterate(iters)
+        got = e.digits()
+    o = oracle_mod.Oracle(p, mode)
+    o.iterate(iters)
+    _cmp(got, o.digits(), f"large p={p} mode={mode}")
+
+
+@pytest.mark.parametrize("p", [9941, 44497, 132049])
+def test_paths_agree(m2, p):
+    """The one-CTA path and the three-pass path give the same state."""
+    with m2.Engine(p, m2.MODE_PRP, path=m2.PATH_SMALL) as a, m2.Engine(p, m2.MODE_PRP, path=m2.PATH_LARGE) as b:
+        for _ in range(3):
+            a.iterate(500)
+            b.iterate(500)
+            _cmp(a.digits(), b.digits(), f"paths p={p}")
