@@ -1,0 +1,405 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Lucas-Lehmer / PRP engine.
+
+Headline: ms per squaring iteration of the PRP test of p = 57885161 (transform
+n = 2^21 digits, 25 MB of dual-field state), the configuration the reference's
+README lists as its large example (README.md:58).  A "step" is one report batch
+of --iters-per-step squarings (the reference synchronises once per report batch,
+mersenne2_gpu.cpp:4803-4853); L2 is flushed (a 256 MB write, larger than the
+129 MB L2) between timed steps, outside the CUDA events.
+
+Also reported:
+  e2e       the same metric through the C ABI with host buffers: every step
+            uploads the digits (m2_set_digits), iterates, and reads the
+            canonical digits back (m2_get_digits), copies inside the timed region
+  roofline  the dominant kernel's algorithmic bytes / CUDA-event time against
+            the measured HBM copy bandwidth; roofline_imad: integer-product
+            count against the measured mad.wide.u32 peak
+  cpu_baseline  the reference's own kernels on the host cores (oracle/_ref),
+            bounded sample
+  batched   config "4096 seeded PRP tests, p in [3, 159739]" through the batched
+            engine vs one test at a time (sampled), res64 bit-exact
+  parity    res64 at iterations 1000 and 10000 against GMP golden values
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+DEFAULT_P = 57885161
+WORKLOAD = "PRP p=57885161 (n=2^21 digits, h=2^20 dual-field elements)"
+METRIC = "ms/iter at N=2^21 (p=57885161)"
+GOLDEN_LARGE = os.path.join(ROOT, "tests", "golden", "large.json")
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC = os.path.join(ROOT, "profiles", "traffic.json")
+L2_FLUSH_BYTES = 256 << 20
+
+
+def _env_int(k: str, d: int) -> int:
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+class Dist:
+    def __init__(self):
+        self.world = _env_int("WORLD_SIZE", 1)
+        self.rank = _env_int("RANK", 0)
+        self.local = _env_int("LOCAL_RANK", 0)
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            backend = "nccl" if _cuda_ok() else "gloo"
+            dist.init_process_group(backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg is not None:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if self.pg is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda" if _cuda_ok() else "cpu")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg is not None:
+            self.pg.destroy_process_group()
+
+
+def _cuda_ok() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _load_json(path: str):
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+def wide_mul_count(h: int) -> int:
+    """32x32->64-bit products of one squaring: 15 per dual-field GF multiplication,
+    G(h) = 0.75 h log2 h + 2 h GF multiplications (forward + inverse radix-4 + centre)."""
+    lg = h.bit_length() - 1
+    return int(15 * (0.75 * h * lg + 2 * h))
+
+
+# ---------------------------------------------------------------- reference arm
+def reference_sample(p: int, iters: int) -> tuple[float, int, float]:
+    """(ms per iteration, threads, setup seconds) of the reference's own kernels on the host."""
+    import oracle
+    oracle.build()
+    t0 = time.perf_counter()
+    r = oracle.RefKernels(p, oracle.PRP)
+    setup = time.perf_counter() - t0
+    r.iterate(1)
+    t0 = time.perf_counter()
+    r.iterate(iters)
+    dt = time.perf_counter() - t0
+    return dt / iters * 1e3, oracle.RefKernels.threads(), setup
+
+
+def run_reference(a, dist: Dist) -> dict | None:
+    if dist.rank != 0:
+        return None
+    import oracle
+    if not oracle.ref_available():
+        return {"impl": "reference", "unavailable": "reference kernel sources not extracted (oracle/_ref missing)"}
+    oracle.build()
+    r = oracle.RefKernels(a.p, oracle.PRP)
+    per = a.ref_iters_per_step
+    for _ in range(a.warmup):
+        r.iterate(per)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        r.iterate(per)
+    dt = time.perf_counter() - t0
+    ms_iter = dt / (a.steps * per) * 1e3
+    threads = oracle.RefKernels.threads()
+    sample = f"{a.steps} steps x {per} squarings of p={a.p} (n=2^21) through the reference's generic kernel plan"
+    return {
+        "impl": "reference", "metric": METRIC, "value": ms_iter, "unit": "ms/iter", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": dt / a.steps * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "iters_per_step": per, "l2": "state and tables resident in host memory"},
+        "cpu_baseline": {"value": ms_iter, "unit": "ms/iter", "cores": threads, "kind": "reference", "sample": sample},
+        "e2e": {"value": ms_iter, "unit": "ms/iter", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+# ---------------------------------------------------------------- batched
+def run_batched(count: int, plain_sample: int) -> dict:
+    import mersenne2gpu_gb300 as m2
+    from mersenne2gpu_gb300.workloads import batch_exponents
+    ps = batch_exponents(count)
+    br = m2.batch_run(ps)
+    tests_per_s = count / br.seconds if br.seconds > 0 else None
+    # plain path: one test at a time, a stratified sample over the sorted exponents
+    order = sorted(range(count), key=lambda i: ps[i])
+    pick = [order[int((k + 0.5) * count / plain_sample)] for k in range(plain_sample)]
+    import torch
+    tot, same = 0.0, 0
+    for i in pick:
+        with m2.Engine(ps[i], m2.MODE_PRP) as e:
+            e.sync()
+            t0 = time.perf_counter()
+            e.iterate(ps[i])
+            e.sync()
+            tot += time.perf_counter() - t0
+            same += int(e.res64() == int(br.res64[i]))
+    plain_per_test = tot / plain_sample
+    plain_tests_per_s = 1.0 / plain_per_test if plain_per_test > 0 else None
+    return {
+        "config": f"{count} PRP tests, seeded primes in [3, 159739] (n = 8 ... 4096), full runs",
+        "tests": count, "seconds": br.seconds, "tests_per_s": tests_per_s,
+        "squarings_per_s": br.squarings / br.seconds if br.seconds > 0 else None,
+        "plain_tests_per_s": plain_tests_per_s,
+        "plain_sample": f"{plain_sample} tests one at a time (stratified by p), mean time extrapolated",
+        "speedup_vs_plain": (tests_per_s / plain_tests_per_s) if (tests_per_s and plain_tests_per_s) else None,
+        "bit_exact_vs_plain": f"{same}/{plain_sample}", "buckets": br.buckets, "launches": br.launches,
+        "primes_found": int(br.is_prime.sum()),
+    }
+
+
+# ---------------------------------------------------------------- main arm
+def run_gb300(a, dist: Dist) -> dict | None:
+    import torch
+
+    import mersenne2gpu_gb300 as m2
+    from mersenne2gpu_gb300 import build as b
+    if dist.rank == 0 or dist.world > 1:
+        b.build()
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    eng = m2.Engine(a.p, m2.MODE_PRP, device=dev, stream=stream.cuda_stream)
+    info = eng.info()
+    ips = a.iters_per_step
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{dev}")
+    golden = _load_json(GOLDEN_LARGE) or {}
+    want = {int(k): v for k, v in golden.get(str(a.p), {}).get("prp", {}).items()}
+    parity = {}
+
+    def check(at: int):
+        if at in want:
+            got = f"{eng.res64():016x}"
+            parity[f"res64@{at}"] = "ok" if got == want[at] else f"MISMATCH {got} != {want[at]}"
+
+    for w in range(a.warmup):
+        flush.zero_()
+        eng.iterate(ips)
+        if w == 0 and ips == 1000:
+            check(1000)
+    torch.cuda.synchronize()
+    dist.barrier()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    t0 = time.perf_counter()
+    for i in range(a.steps):
+        flush.zero_()
+        evs[i][0].record(stream)
+        eng.iterate(ips)
+        evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    dev_ms = sum(s.elapsed_time(e) for s, e in evs)
+    total_iters = (a.warmup + a.steps) * ips
+    check(total_iters)
+    dev_ms = dist.max(dev_ms)
+    ms_iter_rank = dev_ms / (a.steps * ips)
+    value = ms_iter_rank / dist.world
+
+    # e2e: through the C ABI with host buffers
+    host = eng.digits()
+    it = eng.info().iteration
+    torch.cuda.synchronize()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for i in range(a.steps):
+        eng.set_digits(host, it)
+        eng.iterate(ips)
+        host = eng.digits()
+        it += ips
+    dist.barrier()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_value = e2e_s * 1e3 / (a.steps * ips) / dist.world
+    h2d = 8 * info.n
+    d2h = 8 * info.n + (8 * info.rows * (info.row_len // info.cols_per_cta) if info.path == m2.PATH_LARGE else 0)
+
+    # per-kernel device times for the roofline
+    stages = eng.profile(a.profile_iters)
+    dom = max(stages, key=lambda s: s["ms_per_launch"])
+    peaks = _load_json(PEAKS) or {}
+    hbm = float(peaks.get("hbm_gbs") or 6800.0)
+    peak_src = "measured" if peaks.get("hbm_gbs") else "fallback"
+    achieved = dom["bytes_per_launch"] / (dom["ms_per_launch"] * 1e-3) / 1e9
+    traffic = (_load_json(TRAFFIC) or {}).get(dom["name"])
+    mul_peak = m2.measure_mul_peak(dev)
+    h = info.n // 2
+    W = wide_mul_count(h)
+    B = 48 * h
+    t_hbm = B / (hbm * 1e9) * 1e3
+    t_mul = W / mul_peak * 1e3
+    eng.close()
+
+    if dist.rank != 0:
+        return None
+    out = {
+        "metric": METRIC, "value": value, "unit": "ms/iter", "n_gpus": a.gpus, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": dev_ms / a.steps, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (fixed exponent, state from x0 = 3)",
+        "config": {"workload": WORKLOAD, "iters_per_step": ips, "path": "three-pass",
+                   "plan": {"rows": info.rows, "row_len": info.row_len, "cols_per_cta": info.cols_per_cta,
+                            "carry_span": info.span},
+                   "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MB write), state stays L2-resident within a step",
+                   "parallelism": "replicas" if dist.world > 1 else "single"},
+        "wall_s": wall,
+        "gpu_launches": eng_launches(a, ips),
+        "clocks": clk,
+        "e2e": {"value": e2e_value, "unit": "ms/iter", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "kernel": dom["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic,
+                     "bytes_per_launch": dom["bytes_per_launch"], "ms_per_launch": dom["ms_per_launch"],
+                     "peak_source": f"{peak_src} hbm_gbs"},
+        "roofline_imad": {"wide_muls_per_iter": W, "peak_products_per_s": mul_peak, "t_mul_ms": t_mul,
+                          "bytes_per_iter": B, "t_hbm_ms": t_hbm, "roofline_ms": max(t_hbm, t_mul),
+                          "frac": max(t_hbm, t_mul) / ms_iter_rank,
+                          "achieved_products_per_s": W / (ms_iter_rank * 1e-3)},
+        "stages": [{k: s[k] for k in ("name", "ms_per_launch", "bytes_per_launch")} for s in stages],
+        "parity": parity or None,
+    }
+    if a.cpu_baseline and dist.world == 1:
+        try:
+            ms, thr, setup = reference_sample(a.p, a.cpu_iters)
+            out["cpu_baseline"] = {"value": ms, "unit": "ms/iter", "cores": thr, "kind": "reference",
+                                   "sample": f"{a.cpu_iters} squarings of p={a.p} (n=2^21) through the reference's "
+                                             f"own kernels on the host cores (table setup {setup:.1f} s untimed)"}
+        except Exception as ex:  # noqa: BLE001
+            out["cpu_baseline"] = {"value": None, "unit": "ms/iter", "cores": 0, "kind": "reference",
+                                   "sample": f"unavailable: {ex}"}
+    if a.batch:
+        try:
+            out["batched"] = run_batched(a.batch_count, a.plain_sample)
+        except Exception as ex:  # noqa: BLE001
+            out["batched"] = {"error": str(ex)}
+    return out
+
+
+def eng_launches(a, ips: int) -> int:
+    return a.steps * 3 * ips   # three kernels per squaring on the three-pass path
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=7)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--p", type=int, default=DEFAULT_P)
+    ap.add_argument("--iters-per-step", type=int, default=1000)
+    ap.add_argument("--ref-iters-per-step", type=int, default=2)
+    ap.add_argument("--profile-iters", type=int, default=50)
+    ap.add_argument("--cpu-iters", type=int, default=8)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-batch", dest="batch", action="store_false")
+    ap.add_argument("--batch-count", type=int, default=4096)
+    ap.add_argument("--plain-sample", type=int, default=8)
+    a = ap.parse_args()
+    if a.warmup < 3:
+        a.warmup = 3
+    dist = Dist()
+    try:
+        res = run_reference(a, dist) if a.impl == "reference" else run_gb300(a, dist)
+    finally:
+        dist.close()
+    if res is not None:
+        print(json.dumps(res), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -104,6 +104,29 @@ int m2_info(m2_ctx* ctx, m2_info_t* info);
 /* Releases everything the context owns (mersenne2_gpu.cpp:4884-4958). */
 void m2_destroy(m2_ctx* ctx);
 
+/* ---------------- profiling ---------------- */
+typedef struct {
+    char name[32];
+    double ms_per_launch;        /* average device time of one launch */
+    uint64_t launches;
+    uint64_t bytes_per_launch;   /* algorithmic bytes the stage must read + write */
+    uint32_t iters_per_launch;   /* squarings one launch performs */
+} m2_stage_time;
+
+/* Runs `iters` squarings with CUDA events around every kernel launch and
+ * reports each stage's average device time.  Counterpart of the reference
+ * prototype's --profile-kernels (gf61_ntt_prp_opencl_inplace_nobitrev_fused_
+ * powonly_blockcarry.cpp:645-698), which sums OpenCL event times per kernel. */
+int m2_profile(m2_ctx* ctx, uint32_t iters, m2_stage_time* out, int max_stages, int* n_stages);
+
+/* Kernel launches that m2_iterate(ctx, k) issues. */
+uint64_t m2_launches_for(m2_ctx* ctx, uint32_t k);
+
+/* Peak rate of 32x32->64-bit integer products (mad.wide.u32) on a device,
+ * products per second: the compute roofline denominator.  No reference
+ * counterpart. */
+int m2_measure_mul_peak(int device, double* products_per_s);
+
 /* Digit widths (n bytes) of exponent p, without a device; and log2 n. */
 int m2_layout(uint32_t p, int* ln, uint64_t* n, uint8_t* widths /* may be NULL */);
 

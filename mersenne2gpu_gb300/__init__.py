@@ -23,6 +23,7 @@ _MODES = {"ll": MODE_LL, "prp": MODE_PRP, "prp3": MODE_PRP3}
 EXPORTS = (
     "m2_create", "m2_iterate", "m2_sync", "m2_get_digits", "m2_set_digits", "m2_res64",
     "m2_verdict", "m2_info", "m2_destroy", "m2_layout", "m2_strerror", "m2_batch_run",
+    "m2_profile", "m2_launches_for", "m2_measure_mul_peak",
 )
 
 
@@ -42,6 +43,11 @@ class _Info(ctypes.Structure):
                 ("iteration", ctypes.c_uint32), ("total_iters", ctypes.c_uint32), ("path", ctypes.c_int),
                 ("rows", ctypes.c_uint32), ("row_len", ctypes.c_uint32), ("cols_per_cta", ctypes.c_uint32),
                 ("span", ctypes.c_uint32), ("device_bytes", ctypes.c_uint64)]
+
+
+class _StageTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("ms_per_launch", ctypes.c_double), ("launches", ctypes.c_uint64),
+                ("bytes_per_launch", ctypes.c_uint64), ("iters_per_launch", ctypes.c_uint32)]
 
 
 class _BatchStats(ctypes.Structure):
@@ -73,8 +79,12 @@ def _lib() -> ctypes.CDLL:
         L.m2_strerror.argtypes = [i]
         L.m2_strerror.restype = ctypes.c_char_p
         L.m2_batch_run.argtypes = [vp, vp, vp, ctypes.c_size_t, vp, vp, i, ctypes.POINTER(_BatchStats)]
+        L.m2_profile.argtypes = [vp, u32, ctypes.POINTER(_StageTime), i, ctypes.POINTER(i)]
+        L.m2_launches_for.argtypes = [vp, u32]
+        L.m2_launches_for.restype = u64
+        L.m2_measure_mul_peak.argtypes = [i, ctypes.POINTER(ctypes.c_double)]
         for name in EXPORTS:
-            if name not in ("m2_destroy", "m2_strerror"):
+            if name not in ("m2_destroy", "m2_strerror", "m2_launches_for"):
                 getattr(L, name).restype = i
         _LIB = L
     return _LIB
@@ -180,11 +190,30 @@ class Engine:
         _check(self._L.m2_verdict(self._h, ctypes.byref(v)), "m2_verdict")
         return bool(v.value)
 
+    def profile(self, iters: int) -> list[dict]:
+        """Per-stage average device time over `iters` squarings (advances the state)."""
+        arr = (_StageTime * 8)()
+        cnt = ctypes.c_int()
+        _check(self._L.m2_profile(self._h, iters, arr, 8, ctypes.byref(cnt)), "m2_profile")
+        return [dict(name=a.name.decode(), ms_per_launch=a.ms_per_launch, launches=a.launches,
+                     bytes_per_launch=a.bytes_per_launch, iters_per_launch=a.iters_per_launch)
+                for a in arr[: cnt.value]]
+
+    def launches_for(self, k: int) -> int:
+        return int(self._L.m2_launches_for(self._h, k))
+
     def run(self) -> bool:
         """Remaining iterations to completion; returns the verdict."""
         i = self.info()
         self.iterate(i.total_iters - i.iteration)
         return self.verdict()
+
+
+def measure_mul_peak(device: int = 0) -> float:
+    """Peak 32x32->64-bit integer products per second on the device."""
+    r = ctypes.c_double()
+    _check(_lib().m2_measure_mul_peak(device, ctypes.byref(r)), "m2_measure_mul_peak")
+    return r.value
 
 
 @dataclass

@@ -338,6 +338,62 @@ void m2_destroy(m2_ctx* c) {
     delete c;
 }
 
+int m2_profile(m2_ctx* c, uint32_t iters, m2_stage_time* out, int max_stages, int* n_stages) {
+    if (!c || !out || max_stages < 1 || iters == 0) return M2_EINVAL;
+    if (cudaSetDevice(c->device) != cudaSuccess) return M2_ECUDA;
+    const int ns = (c->path == M2_PATH_SMALL) ? 1 : m2k::LARGE_STAGES;
+    const uint32_t launches = (c->path == M2_PATH_SMALL) ? 1u : iters;
+    std::vector<cudaEvent_t> ev((size_t)launches * ns + 1);
+    for (auto& e : ev) if (cudaEventCreate(&e) != cudaSuccess) return M2_ECUDA;
+    cudaError_t err = cudaEventRecord(ev[0], c->stream);
+    for (uint32_t it = 0; it < launches && err == cudaSuccess; ++it) {
+        for (int st = 0; st < ns && err == cudaSuccess; ++st) {
+            if (c->path == M2_PATH_SMALL) err = m2k::launch_small(c->d_test, 1, (unsigned)c->L.h, c->threads, iters, c->stream);
+            else err = m2k::launch_large_stage(c->plan, c->bufs, st, c->stream);
+            if (err == cudaSuccess) err = cudaEventRecord(ev[(size_t)it * ns + st + 1], c->stream);
+        }
+    }
+    if (err == cudaSuccess) err = cudaStreamSynchronize(c->stream);
+    std::vector<double> tot(ns, 0.0);
+    if (err == cudaSuccess) {
+        for (uint32_t it = 0; it < launches; ++it)
+            for (int st = 0; st < ns; ++st) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, ev[(size_t)it * ns + st], ev[(size_t)it * ns + st + 1]);
+                tot[st] += ms;
+            }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (err != cudaSuccess) return M2_ECUDA;
+    c->iteration += iters;
+    const int k = std::min(ns, max_stages);
+    for (int st = 0; st < k; ++st) {
+        m2_stage_time& o = out[st];
+        std::memset(&o, 0, sizeof(o));
+        const char* nm = (c->path == M2_PATH_SMALL) ? "k_small" : m2k::large_stage_name(st);
+        std::strncpy(o.name, nm, sizeof(o.name) - 1);
+        o.launches = launches;
+        o.ms_per_launch = tot[st] / launches;
+        o.iters_per_launch = (c->path == M2_PATH_SMALL) ? iters : 1u;
+        o.bytes_per_launch = (c->path == M2_PATH_SMALL) ? 16ull * c->L.n : m2k::large_stage_bytes(c->plan, st);
+    }
+    if (n_stages) *n_stages = k;
+    return M2_OK;
+}
+
+uint64_t m2_launches_for(m2_ctx* c, uint32_t k) {
+    if (!c || k == 0) return 0;
+    return (c->path == M2_PATH_SMALL) ? 1ull : (uint64_t)m2k::LARGE_STAGES * k;
+}
+
+int m2_measure_mul_peak(int device, double* products_per_s) {
+    if (!products_per_s) return M2_EINVAL;
+    const double r = m2k::measure_wide_mul_rate(device);
+    if (r <= 0.0) return M2_ECUDA;
+    *products_per_s = r;
+    return M2_OK;
+}
+
 // ---------------- batched engine ----------------
 // Tests are bucketed by transform length h; every bucket is one persistent
 // launch (CTAs pull test indices from a device counter, longest tests first),

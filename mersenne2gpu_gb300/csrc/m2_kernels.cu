@@ -493,16 +493,42 @@ cudaError_t large_setup(const LargePlan& P) {
     return cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, sr);
 }
 
-cudaError_t launch_large_iteration(const LargePlan& P, const LargeBufs& b, cudaStream_t s) {
+cudaError_t launch_large_stage(const LargePlan& P, const LargeBufs& b, int stage, cudaStream_t s) {
     const size_t sc = large_smem_cols(P), sr = large_smem_rows(P);
+    if (stage == 0) {
 #define M2_FWD(CC) if (P.C == CC) k_cols_fwd<CC><<<P.G, LT, sc, s>>>(P, b);
-    M2_FOR_C(M2_FWD)
+        M2_FOR_C(M2_FWD)
 #undef M2_FWD
-    k_rows<<<P.R / 2, LT, sr, s>>>(P, b);
+    } else if (stage == 1) {
+        k_rows<<<P.R / 2, LT, sr, s>>>(P, b);
+    } else {
 #define M2_INV(CC) if (P.C == CC) k_cols_inv<CC><<<P.G, LT, sc, s>>>(P, b);
-    M2_FOR_C(M2_INV)
+        M2_FOR_C(M2_INV)
 #undef M2_INV
+    }
     return cudaGetLastError();
+}
+
+const char* large_stage_name(int stage) {
+    static const char* names[] = {"k_cols_fwd", "k_rows", "k_cols_inv"};
+    return (stage >= 0 && stage < 3) ? names[stage] : "?";
+}
+
+// Algorithmic bytes of one launch: what the stage must read and write at least.
+unsigned long long large_stage_bytes(const LargePlan& P, int stage) {
+    const unsigned long long h = (unsigned long long)P.R * P.B;
+    const unsigned long long carries = 8ull * P.R * P.G;
+    if (stage == 0) return 16ull * h + carries + 24ull * h;   // digits + carries in, dual elements out
+    if (stage == 1) return 48ull * h;                          // dual elements in and out
+    return 24ull * h + 16ull * h + carries;                    // dual elements in, digits + carries out
+}
+
+cudaError_t launch_large_iteration(const LargePlan& P, const LargeBufs& b, cudaStream_t s) {
+    for (int st = 0; st < LARGE_STAGES; ++st) {
+        cudaError_t e = launch_large_stage(P, b, st, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace m2k

@@ -63,5 +63,13 @@ size_t large_smem_cols(const LargePlan& P);
 size_t large_smem_rows(const LargePlan& P);
 cudaError_t large_setup(const LargePlan& P);   // sets max dynamic smem attributes
 cudaError_t launch_large_iteration(const LargePlan& P, const LargeBufs& b, cudaStream_t s);
+constexpr int LARGE_STAGES = 3;
+cudaError_t launch_large_stage(const LargePlan& P, const LargeBufs& b, int stage, cudaStream_t s);
+const char* large_stage_name(int stage);
+unsigned long long large_stage_bytes(const LargePlan& P, int stage);
+
+// Throughput of 32x32->64-bit integer multiplies (mul.wide.u32 / mad.wide.u32)
+// on every SM: independent chains, returns products per second.
+double measure_wide_mul_rate(int device);
 
 }  // namespace m2k
