@@ -127,6 +127,25 @@ uint64_t m2_launches_for(m2_ctx* ctx, uint32_t k);
  * counterpart. */
 int m2_measure_mul_peak(int device, double* products_per_s);
 
+/* ---------------- squaring without device allocation ----------------
+ * No counterpart in the reference.  For callers that may not call cudaMalloc
+ * (a framework that owns all device memory through its own pool, or a
+ * latency-critical path where an allocation could synchronise the device):
+ * advances the residue held in `digits` -- n signed 64-bit words in DEVICE
+ * memory, value sum digits[j] 2^bitpos_j mod 2^p - 1, |digits[j]| < 2^width_j
+ * (canonical digits qualify) -- by `iters` squarings of `mode` in place, on
+ * `stream` (NULL = the legacy default stream) of the current device, and
+ * returns when they are done.  Output digits represent the new residue with
+ * |digits[j]| <= 2^(width_j - 1) + 8 (not canonical: one carry pass with
+ * wrap-around, on the host or the device, makes them canonical).
+ * All scratch (element arrays, carries, tables: at most 8 MiB) is one static
+ * device array that every GPU loading the library holds until exit; the
+ * transform must satisfy 128 <= n <= 2^18 (2689 <= p <= 9437179), larger or
+ * smaller exponents return M2_EUNSUPPORTED.  Every call shares that array:
+ * calls whose work overlaps on the GPU race.  The first call on a device looks
+ * up the array's device address; make it before any stream capture. */
+int m2_square_noalloc(uint32_t p, int mode, int64_t* digits, uint32_t iters, void* stream);
+
 /* Digit widths (n bytes) of exponent p, without a device; and log2 n. */
 int m2_layout(uint32_t p, int* ln, uint64_t* n, uint8_t* widths /* may be NULL */);
 

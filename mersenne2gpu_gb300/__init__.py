@@ -23,7 +23,7 @@ _MODES = {"ll": MODE_LL, "prp": MODE_PRP, "prp3": MODE_PRP3}
 EXPORTS = (
     "m2_create", "m2_iterate", "m2_sync", "m2_get_digits", "m2_set_digits", "m2_res64",
     "m2_verdict", "m2_info", "m2_destroy", "m2_layout", "m2_strerror", "m2_batch_run",
-    "m2_profile", "m2_launches_for", "m2_measure_mul_peak",
+    "m2_profile", "m2_launches_for", "m2_measure_mul_peak", "m2_square_noalloc",
 )
 
 
@@ -83,6 +83,7 @@ def _lib() -> ctypes.CDLL:
         L.m2_launches_for.argtypes = [vp, u32]
         L.m2_launches_for.restype = u64
         L.m2_measure_mul_peak.argtypes = [i, ctypes.POINTER(ctypes.c_double)]
+        L.m2_square_noalloc.argtypes = [u32, i, vp, u32, vp]
         for name in EXPORTS:
             if name not in ("m2_destroy", "m2_strerror", "m2_launches_for"):
                 getattr(L, name).restype = i
