@@ -83,7 +83,8 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
     cli_src = os.path.join(CSRC, "mersenne2_cli.cpp")
     if os.path.exists(cli_src) and (force or _stale(CLI, [cli_src, LIB, os.path.join(ROOT, "include", "m2gpu.h")])):
         _run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-o", CLI, cli_src,
-              "-L", PKG, "-lm2gpu", f"-Wl,-rpath,{PKG}", "-Wl,-rpath,$ORIGIN"], verbose)
+              "-I", "/usr/local/cuda/include", "-L", PKG, "-lm2gpu", "-L", "/usr/local/cuda/lib64", "-lcudart",
+              f"-Wl,-rpath,{PKG}", "-Wl,-rpath,$ORIGIN"], verbose)
     return LIB
 
 

@@ -376,6 +376,7 @@ u64 o_res64(const o_ctx* c) {
 /* 1 = prime / probable prime (M2:4865-4868, 3051-3076; PRP-3: == 3) */
 int o_verdict(const o_ctx* c) {
     u64 want = (c->mode == O_LL) ? 0 : (c->mode == O_PRP ? 9 : 3);
+    if (c->p < 64) want %= (((u64)1) << c->p) - 1;     /* 9 mod 7 = 2 for p = 3 */
     if (is_all_ones(c)) return want == 0;
     u64 r = 0; unsigned pos = 0;
     for (u64 j = 0; j < c->n; ++j) {

@@ -1,0 +1,102 @@
+"""Host-side logic and the C ABI surface, no GPU needed (no compute calls)."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+# The reference's exponent -> n table (README.md:69-102); rows 1-2 of the README
+# (3-173 -> 4, 179-349 -> 8) disagree with its own code, which gives n = 8 for
+# every exponent up to 349 (mersenne2_gpu.cpp:286-293): the code is authoritative.
+README_TABLE = [
+    (3, 173, 8), (179, 349, 8), (353, 683, 16), (691, 1373, 32), (1381, 2687, 64), (2689, 5351, 128),
+    (5381, 10487, 256), (10499, 20983, 512), (21001, 40949, 1024), (40961, 81919, 2048), (81929, 159739, 4096),
+    (159763, 319483, 8192), (319489, 622577, 16384), (622603, 1245169, 32768), (1245187, 2424827, 65536),
+    (2424833, 4849651, 131072), (4849687, 9437179, 262144), (9437189, 18874367, 524288),
+    (18874379, 36700159, 1048576), (36700201, 73400311, 2097152), (73400329, 142606333, 4194304),
+    (142606357, 285212659, 8388608), (285212677, 553648103, 16777216), (553648171, 1107296251, 33554432),
+    (1107296257, 2147483647, 67108864),
+]
+
+
+def test_transform_table(m2, oracle_mod):
+    for lo, hi, n in README_TABLE:
+        for p in (lo, hi):
+            ln, nn, _ = m2.layout(p) if p < 40_000_000 else (None, None, None)
+            want = n.bit_length() - 1
+            assert oracle_mod.transformsize(p) == want, p
+            if ln is not None:
+                assert (ln, nn) == (want, n), p
+
+
+@pytest.mark.parametrize("p", [3, 5, 7, 31, 127, 9941, 132049, 216091, 1398269, 9437179])
+def test_layout_matches_oracle(m2, oracle_mod, p):
+    ln, n, w = m2.layout(p)
+    o = oracle_mod.Oracle(p, 1)
+    assert (ln, n) == (o.ln, o.n)
+    assert np.array_equal(w, o.widths())
+    assert int(w.astype(np.int64).sum()) == p
+    q = p >> ln
+    assert set(np.unique(w).tolist()) <= {q, q + 1}
+
+
+def _header_symbols():
+    src = open(os.path.join(ROOT, "include", "m2gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(m2_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol(m2):
+    syms = _header_symbols()
+    assert "m2_create" in syms and "m2_square_noalloc" in syms
+    lib = m2._lib()
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert sorted(m2.EXPORTS) == syms
+
+
+def test_strerror_codes(m2):
+    lib = m2._lib()
+    for code in range(0, -7, -1):
+        assert lib.m2_strerror(code)
+    assert lib.m2_strerror(-1) == b"invalid argument"
+
+
+def test_invalid_arguments_rejected_without_device(m2):
+    import ctypes
+    lib = m2._lib()
+    h = ctypes.c_void_p()
+    assert lib.m2_create(ctypes.byref(h), 2, 1, None) == -1     # p < 3
+    assert lib.m2_create(ctypes.byref(h), 9941, 7, None) == -1  # bad mode
+    assert lib.m2_iterate(None, 1) == -1
+    assert lib.m2_layout(1, None, None, None) == -1
+
+
+def _cli():
+    return os.path.join(ROOT, "mersenne2gpu_gb300", "mersenne2")
+
+
+def test_cli_usage_and_argument_errors(m2):
+    exe = _cli()
+    assert os.path.exists(exe)
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 1 and "Usage:" in r.stderr and "[ll|prp] [report_every]" in r.stderr
+    r = subprocess.run([exe, "9941", "prp", "100", "junk"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Unknown argument: junk" in r.stderr
+    r = subprocess.run([exe, "9941", "-d"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Missing device id after -d" in r.stderr
+    r = subprocess.run([exe, "9941", "-B"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Missing carry_pairs after -B" in r.stderr
+
+
+def test_cli_first_line_without_gpu(m2):
+    """The transform line comes before any device work (mersenne2_gpu.cpp:3733)."""
+    from conftest import have_gpu
+    if have_gpu():
+        pytest.skip("a GPU is present; covered by the GPU CLI test")
+    r = subprocess.run([_cli(), "57885161", "prp"], capture_output=True, text=True)
+    assert r.stdout.splitlines()[0] == "p=57885161, ln=21, transform=1048576 (n=2097152)"
+    assert r.returncode == 1
