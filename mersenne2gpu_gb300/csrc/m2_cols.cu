@@ -1,0 +1,279 @@
+// m2_cols.cu -- column passes of the three-pass path for R = 1024 rows and
+// C = 4 columns per CTA (the plans of n = 2^21 and 2^22), with the radix-16
+// passes spread over lane quads as in the row pass.
+//
+// k_cols_fwd_q (one CTA per group of 4 columns, 512 threads):
+//   row stage  each thread takes whole rows: applies the segment carry that
+//              the previous k_cols_inv_q left for the row's 8 digits (the carry
+//              of the segment before it), converts to both fields and weights;
+//   pass A     levels 1-2 of the columns (radix 16 in a lane quad);
+//   pass B     levels 3-4;
+//   pass C     level 5 on groups of 4 consecutive rows, stored to global memory.
+// k_cols_inv_q runs pass C (from global), B and A inverse, then the row stage
+// unweights, recombines (CRT) and carries each row segment of 8 digits,
+// writing digits and the segment's carry out.
+//
+// Shared memory: 6 arrays of 32-bit words, element (row r, column c) at
+// r C + c through an XOR swizzle of the low five address bits (by bits 5-11)
+// that keeps every warp access of these stages on 32 distinct banks.
+#include "m2_field.cuh"
+#include "m2_kernels.cuh"
+
+using namespace m2d;
+
+namespace m2k {
+
+namespace {
+
+constexpr int CR = 1024, CC = 4, CNT = 512;
+
+__device__ __forceinline__ u32 swzc(u32 e) {
+    u32 x = 0;
+    x ^= (0u - ((e >> 5) & 1u)) & 26u;
+    x ^= (0u - ((e >> 6) & 1u)) & 31u;
+    x ^= (0u - ((e >> 7) & 1u)) & 18u;
+    x ^= (0u - ((e >> 8) & 1u)) & 25u;
+    x ^= (0u - ((e >> 9) & 1u)) & 14u;
+    x ^= (0u - ((e >> 10) & 1u)) & 10u;
+    x ^= (0u - ((e >> 11) & 1u)) & 31u;
+    return e ^ x;
+}
+
+struct S6c {
+    u32 *al, *ah, *bl, *bh, *c, *d;
+    __device__ __forceinline__ E ld(u32 e) const {
+        const u32 p = swzc(e);
+        return E{(u64)al[p] | ((u64)ah[p] << 32), (u64)bl[p] | ((u64)bh[p] << 32), c[p], d[p]};
+    }
+    __device__ __forceinline__ void st(u32 e, const E& v) const {
+        const u32 p = swzc(e);
+        al[p] = (u32)v.a; ah[p] = (u32)(v.a >> 32); bl[p] = (u32)v.b; bh[p] = (u32)(v.b >> 32); c[p] = v.c; d[p] = v.d;
+    }
+};
+__device__ __forceinline__ S6c make_s6c(unsigned char* base, u32 ne) {
+    u32* w = reinterpret_cast<u32*>(base);
+    return S6c{w, w + ne, w + 2 * ne, w + 3 * ne, w + 4 * ne, w + 5 * ne};
+}
+
+__device__ __forceinline__ E ldw(const DTw* t, u64 i) {
+    const u64* q = reinterpret_cast<const u64*>(t + i);
+    const u64 a = __ldg(q), b = __ldg(q + 1), cd = __ldg(q + 2);
+    return E{a, b, (u32)cd, (u32)(cd >> 32)};
+}
+struct Tri { E r1, r2, r3; };
+__device__ __forceinline__ Tri tri(const DTw* tw4, u64 S, u64 J) {
+    const u64 base = 3 * (S + J);
+    return Tri{ldw(tw4, base), ldw(tw4, base + 1), ldw(tw4, base + 2)};
+}
+__device__ __forceinline__ E shfl_xor_e(const E& v, int m) {
+    E r;
+    r.a = __shfl_xor_sync(0xffffffffu, v.a, m);
+    r.b = __shfl_xor_sync(0xffffffffu, v.b, m);
+    r.c = __shfl_xor_sync(0xffffffffu, v.c, m);
+    r.d = __shfl_xor_sync(0xffffffffu, v.d, m);
+    return r;
+}
+__device__ __forceinline__ void quad_transpose(E (&x)[4], u32 l) {
+    {
+        const bool hi = (l & 2u) != 0;
+        const E s0 = hi ? x[0] : x[2], s1 = hi ? x[1] : x[3];
+        const E r0 = shfl_xor_e(s0, 2), r1 = shfl_xor_e(s1, 2);
+        if (hi) { x[0] = r0; x[1] = r1; } else { x[2] = r0; x[3] = r1; }
+    }
+    {
+        const bool hi = (l & 1u) != 0;
+        const E s0 = hi ? x[0] : x[1], s1 = hi ? x[2] : x[3];
+        const E r0 = shfl_xor_e(s0, 1), r1 = shfl_xor_e(s1, 1);
+        if (hi) { x[0] = r0; x[2] = r1; } else { x[1] = r0; x[3] = r1; }
+    }
+}
+
+__device__ __forceinline__ u64 bitpos(u32 p, int ln, u64 j) { return j ? ((((u64)p * j) - 1) >> ln) + 1 : 0; }
+__device__ __forceinline__ u32 width_of(u32 p, int ln, u64 j) { return (u32)(bitpos(p, ln, j + 1) - bitpos(p, ln, j)); }
+__device__ __forceinline__ E weigh(i64 d0, i64 d1, u32 s061, u32 s161, u32 s031, u32 s131) {
+    return E{rotl61(digit_to61(d0), s061), rotl61(digit_to61(d1), s161), rotl31(digit_to31(d0), s031), rotl31(digit_to31(d1), s131)};
+}
+__device__ __forceinline__ u32 unrot61(u32 s, int ln) { const u32 t = (s + (u32)ln + 1u) % 61u; return t ? 61u - t : 0u; }
+__device__ __forceinline__ u32 unrot31(u32 s, int ln) { const u32 t = (s + (u32)ln + 1u) % 31u; return t ? 31u - t : 0u; }
+__device__ __forceinline__ bool fits64(i128 c) { const i128 hi = c >> 63; return hi == 0 || hi == -1; }
+
+// the 16-element sub-column passes over the columns (rows i + stride k of a block)
+__device__ __forceinline__ void colpass_fwd(const S6c& z, u32 base, u32 stride, u32 l, const DTw* tw4, u64 SA_, u64 JA, u64 JB0) {
+    E x[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) x[m] = z.ld(base + stride * (l + 4 * m));
+    { const Tri A = tri(tw4, SA_, JA); dif4(x[0], x[1], x[2], x[3], A.r1, A.r2, A.r3); }
+    quad_transpose(x, l);
+    { const Tri Bt = tri(tw4, 4 * SA_, JB0 + l); dif4(x[0], x[1], x[2], x[3], Bt.r1, Bt.r2, Bt.r3); }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) z.st(base + stride * (4 * l + m), x[m]);
+}
+__device__ __forceinline__ void colpass_inv(const S6c& z, u32 base, u32 stride, u32 l, const DTw* tw4, u64 SA_, u64 JA, u64 JB0) {
+    E x[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) x[m] = z.ld(base + stride * (4 * l + m));
+    { const Tri Bt = tri(tw4, 4 * SA_, JB0 + l); dit4(x[0], x[1], x[2], x[3], Bt.r1, Bt.r2, Bt.r3); }
+    quad_transpose(x, l);
+    { const Tri A = tri(tw4, SA_, JA); dit4(x[0], x[1], x[2], x[3], A.r1, A.r2, A.r3); }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) z.st(base + stride * (l + 4 * m), x[m]);
+}
+
+}  // namespace
+
+// element (row r, column c) of the CTA's column group lives at r*CC + c
+__global__ void __launch_bounds__(CNT, 2) k_cols_fwd_q(LargePlan P, LargeBufs bf) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const S6c z = make_s6c(smem, CR * CC);
+    const u32 B = P.B, G = P.G, g = blockIdx.x, tid = threadIdx.x;
+    const u64 RG = (u64)CR * G;
+    const u32 p = P.p;
+    const int ln = P.ln;
+    // row stage: pending carry, fields, weights
+#pragma unroll 1
+    for (u32 r = tid; r < (u32)CR; r += CNT) {
+        const u64 s = (u64)r * G + g;
+        i64 c = bf.carries[(s + RG - 1) % RG];
+        const u64 j0 = 2 * ((u64)r * B + (u64)g * CC);
+        i64 d[2 * CC];
+        const longlong2* src = reinterpret_cast<const longlong2*>(bf.digits + j0);
+#pragma unroll
+        for (int u = 0; u < CC; ++u) { const longlong2 v = src[u]; d[2 * u] = v.x; d[2 * u + 1] = v.y; }
+#pragma unroll
+        for (int u = 0; u < 2 * CC; ++u) {
+            if (u < P.span) d[u] = split_balanced64(d[u] + c, width_of(p, ln, j0 + u), c);
+            else if (u == P.span) d[u] += c;
+        }
+        const uchar4* w61 = reinterpret_cast<const uchar4*>(bf.w61 + j0);
+        const uchar4* w31 = reinterpret_cast<const uchar4*>(bf.w31 + j0);
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+            const uchar4 a = w61[h2], b = w31[h2];
+            z.st(r * CC + 2 * h2, weigh(d[4 * h2], d[4 * h2 + 1], a.x, a.y, b.x, b.y));
+            z.st(r * CC + 2 * h2 + 1, weigh(d[4 * h2 + 2], d[4 * h2 + 3], a.z, a.w, b.z, b.w));
+        }
+    }
+    __syncthreads();
+    const u32 l = tid & 3u;
+    // pass A: levels 1-2 (blocks of 1024 and 256 rows)
+#pragma unroll 1
+    for (u32 L = tid; L < (u32)(CC * CR / 4); L += CNT) {
+        const u32 sc = L >> 2, c = sc % CC, i = sc / CC;
+        colpass_fwd(z, i * CC + c, (CR / 16) * CC, l, bf.tw4, 1, 0, 0);
+    }
+    __syncthreads();
+    // pass B: levels 3-4 (blocks of 64 and 16 rows)
+#pragma unroll 1
+    for (u32 L = tid; L < (u32)(CC * CR / 4); L += CNT) {
+        const u32 sc = L >> 2, c = sc % CC, rest = sc / CC, jb = rest / 4, ib = rest % 4;
+        colpass_fwd(z, (jb * 64 + ib) * CC + c, 4 * CC, l, bf.tw4, 16, jb, 4 * jb);
+    }
+    __syncthreads();
+    // pass C: level 5 (blocks of 4 rows), to global memory
+#pragma unroll 1
+    for (u32 Gq = tid; Gq < (u32)(CC * CR / 4); Gq += CNT) {
+        const u32 c = Gq % CC, J = Gq / CC;
+        E x[4];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) x[b] = z.ld((4 * J + b) * CC + c);
+        const Tri t = tri(bf.tw4, 256, J);
+        dif4(x[0], x[1], x[2], x[3], t.r1, t.r2, t.r3);
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const u64 e = (u64)(4 * J + b) * B + (u64)g * CC + c;
+            bf.za[e] = make_ulonglong2(x[b].a, x[b].b);
+            bf.zb[e] = make_uint2(x[b].c, x[b].d);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(CNT, 2) k_cols_inv_q(LargePlan P, LargeBufs bf) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const S6c z = make_s6c(smem, CR * CC);
+    const u32 B = P.B, G = P.G, g = blockIdx.x, tid = threadIdx.x;
+    const u32 p = P.p;
+    const int ln = P.ln;
+    // pass C inverse: level 5, from global memory
+#pragma unroll 1
+    for (u32 Gq = tid; Gq < (u32)(CC * CR / 4); Gq += CNT) {
+        const u32 c = Gq % CC, J = Gq / CC;
+        E x[4];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const u64 e = (u64)(4 * J + b) * B + (u64)g * CC + c;
+            const ulonglong2 va = bf.za[e];
+            const uint2 vb = bf.zb[e];
+            x[b] = E{va.x, va.y, vb.x, vb.y};
+        }
+        const Tri t = tri(bf.tw4, 256, J);
+        dit4(x[0], x[1], x[2], x[3], t.r1, t.r2, t.r3);
+#pragma unroll
+        for (int b = 0; b < 4; ++b) z.st((4 * J + b) * CC + c, x[b]);
+    }
+    __syncthreads();
+    const u32 l = tid & 3u;
+#pragma unroll 1
+    for (u32 L = tid; L < (u32)(CC * CR / 4); L += CNT) {
+        const u32 sc = L >> 2, c = sc % CC, rest = sc / CC, jb = rest / 4, ib = rest % 4;
+        colpass_inv(z, (jb * 64 + ib) * CC + c, 4 * CC, l, bf.tw4, 16, jb, 4 * jb);
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (u32 L = tid; L < (u32)(CC * CR / 4); L += CNT) {
+        const u32 sc = L >> 2, c = sc % CC, i = sc / CC;
+        colpass_inv(z, i * CC + c, (CR / 16) * CC, l, bf.tw4, 1, 0, 0);
+    }
+    __syncthreads();
+    // row stage: unweight, CRT, carry within the row segment of 8 digits
+#pragma unroll 1
+    for (u32 r = tid; r < (u32)CR; r += CNT) {
+        const u64 e0 = (u64)r * B + (u64)g * CC, j0 = 2 * e0;
+        const uchar4* w61 = reinterpret_cast<const uchar4*>(bf.w61 + j0);
+        const uchar4* w31 = reinterpret_cast<const uchar4*>(bf.w31 + j0);
+        i128 c = 0;
+        i64 d[2 * CC];
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+            const uchar4 a = w61[h2], b = w31[h2];
+            const u32 s61[4] = {a.x, a.y, a.z, a.w}, s31[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const u32 cc = 2 * h2 + u;
+                const E v = z.ld(r * CC + cc);
+                const u64 x0 = rotl61(v.a, unrot61(s61[2 * u], ln)), x1 = rotl61(v.b, unrot61(s61[2 * u + 1], ln));
+                const u32 y0 = rotl31(v.c, unrot31(s31[2 * u], ln)), y1 = rotl31(v.d, unrot31(s31[2 * u + 1], ln));
+                i128 z0 = crt_signed(x0, y0), z1 = crt_signed(x1, y1);
+                if (P.mode == PRP3) { z0 *= 3; z1 *= 3; }
+                if (P.mode == LL && e0 + cc == 0) z0 -= 2;
+                const u64 j = j0 + 2 * cc;
+                d[2 * cc] = split_balanced(z0 + c, width_of(p, ln, j), c);
+                d[2 * cc + 1] = split_balanced(z1 + c, width_of(p, ln, j + 1), c);
+            }
+        }
+        longlong2* dst = reinterpret_cast<longlong2*>(bf.digits + j0);
+#pragma unroll
+        for (int u = 0; u < CC; ++u) dst[u] = make_longlong2(d[2 * u], d[2 * u + 1]);
+        if (!fits64(c)) atomicExch(bf.status, ST_CARRY_RANGE);
+        bf.carries[(u64)r * G + g] = (i64)c;
+    }
+}
+
+bool cols_q_supported(const LargePlan& P) { return P.R == (u32)CR && P.C == (u32)CC && P.span < 2 * CC; }
+
+cudaError_t cols_q_setup(const LargePlan& P) {
+    const int sm = (int)(24ull * CR * CC);
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(k_cols_fwd_q, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
+    if ((e = cudaFuncSetAttribute(k_cols_inv_q, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
+    if ((e = cudaFuncSetAttribute(k_cols_fwd_q, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
+    return cudaFuncSetAttribute(k_cols_inv_q, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+}
+
+cudaError_t launch_cols_q(const LargePlan& P, const LargeBufs& b, bool inverse, cudaStream_t s) {
+    const size_t sm = 24ull * CR * CC;
+    if (inverse) k_cols_inv_q<<<P.G, CNT, sm, s>>>(P, b);
+    else k_cols_fwd_q<<<P.G, CNT, sm, s>>>(P, b);
+    return cudaGetLastError();
+}
+
+}  // namespace m2k

@@ -265,10 +265,11 @@ int small_ctas_per_sm(unsigned int h, int threads) {
 // =====================================================================
 // three-pass path
 // =====================================================================
-constexpr int LT = 256;   // threads per CTA of the large-path kernels
+constexpr int LT = 256;   // threads per CTA of the row kernel
+constexpr int LTC = 512;  // threads per CTA of the column kernels
 
 template <int C>
-__global__ void __launch_bounds__(LT) k_cols_fwd(LargePlan P, LargeBufs bf) {
+__global__ void __launch_bounds__(LTC, 2) k_cols_fwd(LargePlan P, LargeBufs bf) {
     extern __shared__ __align__(16) unsigned char smem[];
     const u32 R = P.R, B = P.B, G = P.G, g = blockIdx.x;
     const u32 NE = (u32)C * R;
@@ -318,7 +319,7 @@ __global__ void __launch_bounds__(LT) k_cols_fwd(LargePlan P, LargeBufs bf) {
     }
 }
 
-__global__ void __launch_bounds__(LT) k_rows(LargePlan P, LargeBufs bf) {
+__global__ void __launch_bounds__(LT, 4) k_rows(LargePlan P, LargeBufs bf) {
     extern __shared__ __align__(16) unsigned char smem[];
     const u32 B = P.B, NE = 2 * B;
     const SE z = make_se(smem, NE);
@@ -427,7 +428,7 @@ __global__ void __launch_bounds__(LT) k_rows(LargePlan P, LargeBufs bf) {
 }
 
 template <int C>
-__global__ void __launch_bounds__(LT) k_cols_inv(LargePlan P, LargeBufs bf) {
+__global__ void __launch_bounds__(LTC, 2) k_cols_inv(LargePlan P, LargeBufs bf) {
     extern __shared__ __align__(16) unsigned char smem[];
     const u32 R = P.R, B = P.B, G = P.G, g = blockIdx.x;
     const u32 NE = (u32)C * R;
@@ -487,22 +488,29 @@ cudaError_t large_setup(const LargePlan& P) {
     if (P.C == CC) {                                                                                        \
         if ((e = cudaFuncSetAttribute(k_cols_fwd<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, sc))) return e; \
         if ((e = cudaFuncSetAttribute(k_cols_inv<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, sc))) return e; \
+        if ((e = cudaFuncSetAttribute(k_cols_fwd<CC>, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e; \
+        if ((e = cudaFuncSetAttribute(k_cols_inv<CC>, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e; \
     }
     M2_FOR_C(M2_SET)
 #undef M2_SET
+    if (rows_rb_supported(P) && (e = rows_rb_setup(P))) return e;
+    if (cols_q_supported(P) && (e = cols_q_setup(P))) return e;
+    if ((e = cudaFuncSetAttribute(k_rows, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
     return cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, sr);
 }
 
 cudaError_t launch_large_stage(const LargePlan& P, const LargeBufs& b, int stage, cudaStream_t s) {
     const size_t sc = large_smem_cols(P), sr = large_smem_rows(P);
+    if (stage != 1 && cols_q_supported(P)) return launch_cols_q(P, b, stage == 2, s);
     if (stage == 0) {
-#define M2_FWD(CC) if (P.C == CC) k_cols_fwd<CC><<<P.G, LT, sc, s>>>(P, b);
+#define M2_FWD(CC) if (P.C == CC) k_cols_fwd<CC><<<P.G, LTC, sc, s>>>(P, b);
         M2_FOR_C(M2_FWD)
 #undef M2_FWD
     } else if (stage == 1) {
+        if (rows_rb_supported(P)) return launch_rows_rb(P, b, s);
         k_rows<<<P.R / 2, LT, sr, s>>>(P, b);
     } else {
-#define M2_INV(CC) if (P.C == CC) k_cols_inv<CC><<<P.G, LT, sc, s>>>(P, b);
+#define M2_INV(CC) if (P.C == CC) k_cols_inv<CC><<<P.G, LTC, sc, s>>>(P, b);
         M2_FOR_C(M2_INV)
 #undef M2_INV
     }

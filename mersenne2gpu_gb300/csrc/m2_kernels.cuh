@@ -64,6 +64,14 @@ size_t large_smem_rows(const LargePlan& P);
 cudaError_t large_setup(const LargePlan& P);   // sets max dynamic smem attributes
 cudaError_t launch_large_iteration(const LargePlan& P, const LargeBufs& b, cudaStream_t s);
 constexpr int LARGE_STAGES = 3;
+// register-blocked row pass (m2_rows.cu), used for row lengths 1024 and 2048
+bool rows_rb_supported(const LargePlan& P);
+cudaError_t rows_rb_setup(const LargePlan& P);
+cudaError_t launch_rows_rb(const LargePlan& P, const LargeBufs& b, cudaStream_t s);
+// quad-shuffle column passes (m2_cols.cu), used for R = 1024 rows and C = 4
+bool cols_q_supported(const LargePlan& P);
+cudaError_t cols_q_setup(const LargePlan& P);
+cudaError_t launch_cols_q(const LargePlan& P, const LargeBufs& b, bool inverse, cudaStream_t s);
 cudaError_t launch_large_stage(const LargePlan& P, const LargeBufs& b, int stage, cudaStream_t s);
 const char* large_stage_name(int stage);
 unsigned long long large_stage_bytes(const LargePlan& P, int stage);

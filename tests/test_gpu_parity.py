@@ -72,6 +72,20 @@ def test_large_path_vs_oracle(m2, oracle_mod, p, mode):
     _cmp(got, o.digits(), f"large p={p} mode={mode}")
 
 
+@pytest.mark.parametrize("p", [18874367, 36700159, 57885161, 115640321])   # row pass of 1024 / 2048, 1024-row columns
+@pytest.mark.parametrize("mode", [0, 1])
+def test_large_path_long_rows_vs_oracle(m2, oracle_mod, p, mode):
+    iters = 2
+    with m2.Engine(p, mode, path=m2.PATH_LARGE) as e:
+        info = e.info()
+        assert info.row_len in (1024, 2048)
+        e.iterate(iters)
+        got = e.digits()
+    o = oracle_mod.Oracle(p, mode)
+    o.iterate(iters)
+    _cmp(got, o.digits(), f"large p={p} mode={mode}")
+
+
 @pytest.mark.parametrize("p", [9941, 44497, 132049])
 def test_paths_agree(m2, p):
     """The one-CTA path and the three-pass path give the same state."""
