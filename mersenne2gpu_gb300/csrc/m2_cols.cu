@@ -97,6 +97,54 @@ __device__ __forceinline__ u32 unrot61(u32 s, int ln) { const u32 t = (s + (u32)
 __device__ __forceinline__ u32 unrot31(u32 s, int ln) { const u32 t = (s + (u32)ln + 1u) % 31u; return t ? 31u - t : 0u; }
 __device__ __forceinline__ bool fits64(i128 c) { const i128 hi = c >> 63; return hi == 0 || hi == -1; }
 
+// left rotation that multiplies by 2^-(s + ln + 1): s < 61 (31), ln + 1 <= 31
+__device__ __forceinline__ u32 unrot61f(u32 s, u32 ln1) { u32 t = s + ln1; t = t >= 61u ? t - 61u : t; return t ? 61u - t : 0u; }
+__device__ __forceinline__ u32 unrot31f(u32 s, u32 ln1) { u32 t = s + ln1; t = t >= 31u ? t - 31u : t; return t ? 31u - t : 0u; }
+
+// One digit of the carry: z = the signed convolution word with z == r61
+// (mod P61), z == r31 (mod P31), |z| < P61 P31 / 2 (Garner), then
+// t = mul z + c + 2^(w-1), digit = (t mod 2^w) - 2^(w-1), carry out t >> w.
+// The carry out is below 2^62 in magnitude for every exponent of the table,
+// so it is formed from the 128-bit t by a 64-bit funnel shift.  1 <= w <= 63.
+__device__ __forceinline__ i64 crt_digit(u64 r61, u32 r31, u32 w, u32 mul, i64 sub, i64& c, u32& bad) {
+    // canonical residues
+    r61 = (r61 == P61) ? 0 : r61;
+    r31 = (r31 == P31) ? 0 : r31;
+    u64 u = r61 + (P61 - r31);                     // (r61 - r31) mod P61, < 2 P61
+    u = (u >= P61) ? u - P61 : u;
+    u += ((u << 31) & P61) | (u >> 30);            // + u 2^31 (a 61-bit rotation)
+    u = (u >= P61) ? u - P61 : u;                  // u = (r61 - r31) (2^31 + 1) mod P61
+    // L = u P31 + r31 = u 2^31 - u + r31 < P61 P31
+    u64 lo = u << 31, hi = u >> 33;
+    const u64 lo2 = lo - u;
+    hi -= (lo2 > lo);
+    lo = lo2 + r31;
+    hi += (lo < lo2);
+    // signed: z = L - M when L > M/2 (M = P61 P31 = 2^92 - 2^61 - 2^31 + 1)
+    constexpr u64 MLO = 0xdfffffff80000001ull, MHI = 0x000000000fffffffull;   // M
+    constexpr u64 HLO = 0xefffffffc0000000ull, HHI = 0x0000000007ffffffull;   // (M - 1) / 2
+    if (hi > HHI || (hi == HHI && lo > HLO)) {
+        const u64 l2 = lo - MLO;
+        hi = hi - MHI - (l2 > lo);
+        lo = l2;
+    }
+    // t = mul z + c + half  (two's complement in hi:lo)
+    if (mul == 3) {
+        const u64 l3 = lo * 3;
+        hi = hi * 3 + __umul64hi(lo, 3);
+        lo = l3;
+    }
+    const i64 add = c - sub + ((i64)1 << (w - 1));
+    const u64 l4 = lo + (u64)add;
+    hi += (l4 < lo) + (u64)(add >> 63);            // sign-extend add into the high word
+    lo = l4;
+    // t >> w fits in 64 bits iff the high word above bit w-1 is pure sign
+    const i64 top = (i64)hi >> (w - 1);
+    bad |= (u32)(top != 0 && top != -1);
+    c = (i64)((hi << (64 - w)) | (lo >> w));
+    return (i64)(lo & ((1ull << w) - 1)) - ((i64)1 << (w - 1));
+}
+
 // the 16-element sub-column passes over the columns (rows i + stride k of a block)
 __device__ __forceinline__ void colpass_fwd(const S6c& z, u32 base, u32 stride, u32 l, const DTw* tw4, u64 SA_, u64 JA, u64 JB0) {
     E x[4];
@@ -230,7 +278,11 @@ __global__ void __launch_bounds__(CNT, 2) k_cols_inv_q(LargePlan P, LargeBufs bf
         const u64 e0 = (u64)r * B + (u64)g * CC, j0 = 2 * e0;
         const uchar4* w61 = reinterpret_cast<const uchar4*>(bf.w61 + j0);
         const uchar4* w31 = reinterpret_cast<const uchar4*>(bf.w31 + j0);
-        i128 c = 0;
+        const u32 ln1 = (u32)ln + 1u, mul = (P.mode == PRP3) ? 3u : 1u;
+        // digit widths of the segment: bit positions ceil(p j / n) at j0 .. j0 + 8
+        u64 bp = bitpos(p, ln, j0);
+        i64 c = 0;
+        u32 bad = 0;
         i64 d[2 * CC];
 #pragma unroll
         for (int h2 = 0; h2 < 2; ++h2) {
@@ -240,21 +292,21 @@ __global__ void __launch_bounds__(CNT, 2) k_cols_inv_q(LargePlan P, LargeBufs bf
             for (int u = 0; u < 2; ++u) {
                 const u32 cc = 2 * h2 + u;
                 const E v = z.ld(r * CC + cc);
-                const u64 x0 = rotl61(v.a, unrot61(s61[2 * u], ln)), x1 = rotl61(v.b, unrot61(s61[2 * u + 1], ln));
-                const u32 y0 = rotl31(v.c, unrot31(s31[2 * u], ln)), y1 = rotl31(v.d, unrot31(s31[2 * u + 1], ln));
-                i128 z0 = crt_signed(x0, y0), z1 = crt_signed(x1, y1);
-                if (P.mode == PRP3) { z0 *= 3; z1 *= 3; }
-                if (P.mode == LL && e0 + cc == 0) z0 -= 2;
+                const u64 x0 = rotl61(v.a, unrot61f(s61[2 * u], ln1)), x1 = rotl61(v.b, unrot61f(s61[2 * u + 1], ln1));
+                const u32 y0 = rotl31(v.c, unrot31f(s31[2 * u], ln1)), y1 = rotl31(v.d, unrot31f(s31[2 * u + 1], ln1));
                 const u64 j = j0 + 2 * cc;
-                d[2 * cc] = split_balanced(z0 + c, width_of(p, ln, j), c);
-                d[2 * cc + 1] = split_balanced(z1 + c, width_of(p, ln, j + 1), c);
+                const u64 bp1 = bitpos(p, ln, j + 1), bp2 = bitpos(p, ln, j + 2);
+                const i64 sub = (P.mode == LL && j == 0) ? 2 : 0;
+                d[2 * cc] = crt_digit(x0, y0, (u32)(bp1 - bp), mul, sub, c, bad);
+                d[2 * cc + 1] = crt_digit(x1, y1, (u32)(bp2 - bp1), mul, 0, c, bad);
+                bp = bp2;
             }
         }
         longlong2* dst = reinterpret_cast<longlong2*>(bf.digits + j0);
 #pragma unroll
         for (int u = 0; u < CC; ++u) dst[u] = make_longlong2(d[2 * u], d[2 * u + 1]);
-        if (!fits64(c)) atomicExch(bf.status, ST_CARRY_RANGE);
-        bf.carries[(u64)r * G + g] = (i64)c;
+        if (bad) atomicExch(bf.status, ST_CARRY_RANGE);
+        bf.carries[(u64)r * G + g] = c;
     }
 }
 
