@@ -19,6 +19,10 @@ Also reported:
             bounded sample
   batched   config "4096 seeded PRP tests, p in [3, 159739]" through the batched
             engine vs one test at a time (sampled), res64 bit-exact
+  serving   seeded Poisson stream of PRP requests, p log-uniform in
+            [1000, 18874367], continuous batching under an HBM budget for a
+            fixed window: p50/p99 time-to-result per transform size,
+            squarings/s, completed results re-run alone
   parity    res64 at iterations 1000 and 10000 against GMP golden values
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
@@ -366,6 +370,12 @@ def run_gb300(a, dist: Dist) -> dict | None:
             out["batched"] = run_batched(a.batch_count, a.plain_sample)
         except Exception as ex:  # noqa: BLE001
             out["batched"] = {"error": str(ex)}
+    if a.serve:
+        try:
+            from mersenne2gpu_gb300.serve import run_serving
+            out["serving"] = run_serving(rate_per_s=a.serve_rate, window_s=a.serve_window, device=dev)
+        except Exception as ex:  # noqa: BLE001
+            out["serving"] = {"error": str(ex)}
     return out
 
 
@@ -388,6 +398,9 @@ def main() -> int:
     ap.add_argument("--no-batch", dest="batch", action="store_false")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--plain-sample", type=int, default=8)
+    ap.add_argument("--no-serve", dest="serve", action="store_false")
+    ap.add_argument("--serve-rate", type=float, default=4.0)
+    ap.add_argument("--serve-window", type=float, default=20.0)
     a = ap.parse_args()
     if a.warmup < 3:
         a.warmup = 3

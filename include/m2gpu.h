@@ -104,6 +104,48 @@ int m2_info(m2_ctx* ctx, m2_info_t* info);
 /* Releases everything the context owns (mersenne2_gpu.cpp:4884-4958). */
 void m2_destroy(m2_ctx* ctx);
 
+/* ---------------- serving engine ----------------
+ * No reference counterpart (the reference tests one exponent per process,
+ * mersenne2_gpu.cpp:3618-4959).  Continuous batching of independent tests on
+ * one GPU: submitted tests wait in a FIFO queue and are admitted while their
+ * device memory fits the budget; every m2_srv_step advances each admitted test
+ * by up to `quantum` squarings -- tests of one transform size on the one-CTA
+ * path share one persistent launch, larger tests run on their own streams, all
+ * concurrently -- then retires the finished tests and frees their memory.
+ * Results of a test are identical to running it alone (m2_create/m2_iterate).
+ * Times are seconds since m2_srv_create (host steady clock). */
+typedef struct m2_server m2_server;
+
+typedef struct {
+    uint64_t id;
+    uint32_t p;
+    int mode;
+    uint32_t iters;          /* squarings performed */
+    uint64_t res64;
+    int is_prime;            /* verdict (meaningful when iters is the full test) */
+    int status;              /* M2_OK or an error code */
+    uint64_t n;              /* transform length */
+    double t_submit, t_admit, t_done;
+} m2_srv_result;
+
+typedef struct {
+    uint32_t queued, active;
+    uint64_t resident_bytes, budget_bytes;
+    uint64_t squarings;      /* squarings performed since creation */
+    uint64_t completed;
+    uint32_t steps, launches;
+} m2_srv_stats;
+
+int m2_srv_create(m2_server** out, int device, uint64_t budget_bytes, uint32_t quantum);
+/* iters = 0 runs the full test (p-2 / p / p-1 squarings) */
+int m2_srv_submit(m2_server* s, uint64_t id, uint32_t p, int mode, uint32_t iters);
+/* one scheduling round: admit, advance every active test, retire finished ones */
+int m2_srv_step(m2_server* s);
+/* copies up to max finished results (oldest first) and removes them */
+int m2_srv_poll(m2_server* s, m2_srv_result* out, int max, int* n_out);
+int m2_srv_stats_get(m2_server* s, m2_srv_stats* st);
+void m2_srv_destroy(m2_server* s);
+
 /* ---------------- profiling ---------------- */
 typedef struct {
     char name[32];
@@ -150,6 +192,10 @@ int m2_square_noalloc(uint32_t p, int mode, int64_t* digits, uint32_t iters, voi
 int m2_layout(uint32_t p, int* ln, uint64_t* n, uint8_t* widths /* may be NULL */);
 
 const char* m2_strerror(int code);
+
+/* Where the most recent CUDA failure of the calling thread happened and the
+ * runtime's description of it ("" when none). */
+const char* m2_last_error(void);
 
 /* ---------------- batched engine ----------------
  * Runs `count` independent tests to completion (or `iters[i]` squarings when

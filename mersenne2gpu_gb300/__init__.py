@@ -24,12 +24,15 @@ EXPORTS = (
     "m2_create", "m2_iterate", "m2_sync", "m2_get_digits", "m2_set_digits", "m2_res64",
     "m2_verdict", "m2_info", "m2_destroy", "m2_layout", "m2_strerror", "m2_batch_run",
     "m2_profile", "m2_launches_for", "m2_measure_mul_peak", "m2_square_noalloc",
+    "m2_srv_create", "m2_srv_submit", "m2_srv_step", "m2_srv_poll", "m2_srv_stats_get", "m2_srv_destroy",
+    "m2_last_error",
 )
 
 
 class M2Error(RuntimeError):
     def __init__(self, code: int, what: str):
-        super().__init__(f"{what}: {_lib().m2_strerror(code).decode()} ({code})")
+        detail = _lib().m2_last_error().decode() if code in (-2, -3) else ""
+        super().__init__(f"{what}: {_lib().m2_strerror(code).decode()} ({code})" + (f" [{detail}]" if detail else ""))
         self.code = code
 
 
@@ -84,8 +87,10 @@ def _lib() -> ctypes.CDLL:
         L.m2_launches_for.restype = u64
         L.m2_measure_mul_peak.argtypes = [i, ctypes.POINTER(ctypes.c_double)]
         L.m2_square_noalloc.argtypes = [u32, i, vp, u32, vp]
+        L.m2_last_error.argtypes = []
+        L.m2_last_error.restype = ctypes.c_char_p
         for name in EXPORTS:
-            if name not in ("m2_destroy", "m2_strerror", "m2_launches_for"):
+            if name not in ("m2_destroy", "m2_strerror", "m2_launches_for", "m2_last_error") and not name.startswith("m2_srv"):
                 getattr(L, name).restype = i
         _LIB = L
     return _LIB

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -14,6 +15,8 @@
 #include <stdexcept>
 #include <tuple>
 #include <vector>
+#include <chrono>
+#include <deque>
 
 using m2::i64;
 using m2::u32;
@@ -48,6 +51,14 @@ int get_twiddles(int device, u64 h, TwTables& out) {
     g_tw[{device, h}] = t;
     out = t;
     return M2_OK;
+}
+
+thread_local char g_last_error[256] = "";
+
+// records where a CUDA call failed (readable through m2_last_error) and maps the code
+int fail_cuda(const char* where, cudaError_t e) {
+    std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s", where, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? M2_ENOMEM : M2_ECUDA;
 }
 
 u32 total_iters_for(u32 p, int mode) {
@@ -86,6 +97,7 @@ struct m2_ctx {
     long long* d_digits = nullptr;
     // small path
     m2k::SmallTest* d_test = nullptr;
+    m2k::SmallTest h_test{};   // host copy of the descriptor (the serving engine batches these)
     int threads = 0;
     int carry_threads = 0;
     // large path
@@ -158,6 +170,8 @@ int read_canonical(m2_ctx* c, std::vector<u64>& out) {
 
 extern "C" {
 
+const char* m2_last_error(void) { return g_last_error; }
+
 const char* m2_strerror(int code) {
     switch (code) {
         case M2_OK: return "ok";
@@ -229,6 +243,7 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
         t.p = p; t.iters = 0; t.ln = raw->L.ln; t.mode = mode; t.span = raw->span;
         t.carry_threads = raw->carry_threads;
         if (cudaMemcpy(raw->d_test, &t, sizeof(t), cudaMemcpyHostToDevice) != cudaSuccess) { m2_destroy(c.release()); return M2_ECUDA; }
+        raw->h_test = t;
     } else {
         const m2k::LargePlan& P = raw->plan;
         raw->plan.mode = mode;
@@ -257,7 +272,7 @@ int m2_iterate(m2_ctx* c, uint32_t k) {
     } else {
         for (uint32_t i = 0; i < k && e == cudaSuccess; ++i) e = m2k::launch_large_iteration(c->plan, c->bufs, c->stream);
     }
-    if (e != cudaSuccess) return M2_ECUDA;
+    if (e != cudaSuccess) return fail_cuda("m2_iterate launch", e);
     c->iteration += k;
     return M2_OK;
 }
@@ -530,6 +545,220 @@ int m2_batch_run(const uint32_t* p, const int* modes, const uint32_t* iters, siz
         stats->buckets = (uint32_t)buckets.size();
     }
     return status_any ? M2_ESTATE : M2_OK;
+}
+
+}  // extern "C"
+
+// ---------------- serving engine ----------------
+namespace {
+
+struct SrvItem {
+    uint64_t id = 0;
+    uint32_t p = 0;
+    int mode = 0;
+    uint32_t total = 0, done = 0;
+    m2_ctx* ctx = nullptr;
+    uint64_t bytes = 0;
+    double t_submit = 0, t_admit = 0;
+};
+
+struct SrvBucket {
+    m2k::SmallTest* d_tests = nullptr;
+    size_t cap = 0;
+    cudaStream_t stream = nullptr;
+};
+
+// device memory a test will hold (digits, weights, status, descriptor; the
+// element arrays and carries of the three-pass path); twiddles are shared
+uint64_t srv_estimate(uint32_t p) {
+    const int ln = m2::transform_log2(p);
+    const uint64_t n = uint64_t(1) << ln, h = n / 2;
+    uint64_t b = 10 * n + 512;
+    if (h > 8192) b += 24 * h + 8 * (h / 4) + 4096;
+    return b;
+}
+
+}  // namespace
+
+struct m2_server {
+    int device = 0;
+    uint64_t budget = 0;
+    uint32_t quantum = 1000;
+    std::deque<SrvItem> queue;
+    std::vector<SrvItem> active;
+    std::deque<m2_srv_result> finished;
+    std::map<u64, SrvBucket> buckets;
+    uint64_t resident = 0, squarings = 0, completed = 0;
+    uint32_t steps = 0, launches = 0;
+    std::chrono::steady_clock::time_point t0;
+    double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+};
+
+namespace {
+
+void srv_retire(m2_server* s, SrvItem& it, int status) {
+    m2_srv_result r{};
+    r.id = it.id; r.p = it.p; r.mode = it.mode; r.iters = it.done; r.status = status;
+    r.t_submit = it.t_submit; r.t_admit = it.t_admit;
+    if (it.ctx) {
+        r.n = it.ctx->L.n;
+        if (status == M2_OK) {
+            int rc = m2_res64(it.ctx, &r.res64);
+            if (rc == M2_OK) rc = m2_verdict(it.ctx, &r.is_prime);
+            r.status = rc;
+        }
+        m2_destroy(it.ctx);
+        it.ctx = nullptr;
+    }
+    r.t_done = s->now();
+    s->resident -= it.bytes;
+    s->completed++;
+    s->finished.push_back(r);
+}
+
+}  // namespace
+
+extern "C" {
+
+int m2_srv_create(m2_server** out, int device, uint64_t budget_bytes, uint32_t quantum) {
+    if (!out || budget_bytes == 0) return M2_EINVAL;
+    if (cudaSetDevice(device) != cudaSuccess) { cudaGetLastError(); return M2_EINVAL; }
+    m2_server* s = new (std::nothrow) m2_server();
+    if (!s) return M2_ENOMEM;
+    s->device = device;
+    s->budget = budget_bytes;
+    s->quantum = quantum ? quantum : 1000;
+    s->t0 = std::chrono::steady_clock::now();
+    *out = s;
+    return M2_OK;
+}
+
+int m2_srv_submit(m2_server* s, uint64_t id, uint32_t p, int mode, uint32_t iters) {
+    if (!s || p < 3 || mode < M2_MODE_LL || mode > M2_MODE_PRP3) return M2_EINVAL;
+    if (m2::transform_log2(p) > 30) return M2_EUNSUPPORTED;
+    SrvItem it;
+    it.id = id; it.p = p; it.mode = mode;
+    const uint32_t full = total_iters_for(p, mode);
+    it.total = iters ? std::min(iters, full) : full;
+    it.bytes = srv_estimate(p);
+    it.t_submit = s->now();
+    s->queue.push_back(it);
+    return M2_OK;
+}
+
+int m2_srv_step(m2_server* s) {
+    if (!s) return M2_EINVAL;
+    if (cudaSetDevice(s->device) != cudaSuccess) return M2_ECUDA;
+    // admission: FIFO while the next test fits the budget
+    while (!s->queue.empty() && s->resident + s->queue.front().bytes <= s->budget) {
+        SrvItem it = s->queue.front();
+        s->queue.pop_front();
+        m2_opts o{};
+        o.device = s->device;
+        const int rc = m2_create(&it.ctx, it.p, it.mode, &o);
+        it.t_admit = s->now();
+        s->resident += it.bytes;
+        if (rc != M2_OK) { it.ctx = nullptr; srv_retire(s, it, rc); continue; }
+        if (it.total == 0) { srv_retire(s, it, M2_OK); continue; }
+        s->active.push_back(it);
+    }
+    if (s->active.empty()) return M2_OK;
+    s->steps++;
+    // one quantum for every active test: small ones batched per transform size
+    std::map<u64, std::vector<size_t>> small;
+    std::vector<size_t> large;
+    for (size_t i = 0; i < s->active.size(); ++i) {
+        if (s->active[i].ctx->path == M2_PATH_SMALL) small[s->active[i].ctx->L.h].push_back(i);
+        else large.push_back(i);
+    }
+    std::vector<uint32_t> k(s->active.size());
+    for (size_t i = 0; i < s->active.size(); ++i) k[i] = std::min(s->quantum, s->active[i].total - s->active[i].done);
+    int rc = M2_OK;
+    for (auto& kv : small) {
+        SrvBucket& b = s->buckets[kv.first];
+        cudaError_t e;
+        if (!b.stream && (e = cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking)) != cudaSuccess)
+            return fail_cuda("server stream", e);
+        if (b.cap < kv.second.size()) {
+            cudaFree(b.d_tests);
+            b.cap = std::max<size_t>(kv.second.size(), 2 * b.cap);
+            if ((e = cudaMalloc(&b.d_tests, b.cap * sizeof(m2k::SmallTest))) != cudaSuccess) { b.cap = 0; return fail_cuda("server descriptors", e); }
+        }
+        std::vector<m2k::SmallTest> desc;
+        for (size_t i : kv.second) {
+            m2k::SmallTest t = s->active[i].ctx->h_test;
+            t.iters = k[i];
+            desc.push_back(t);
+        }
+        if ((e = cudaMemcpyAsync(b.d_tests, desc.data(), desc.size() * sizeof(m2k::SmallTest), cudaMemcpyHostToDevice, b.stream)) != cudaSuccess)
+            return fail_cuda("server descriptor upload", e);
+        const int threads = s->active[kv.second[0]].ctx->threads;
+        if ((e = m2k::launch_small(b.d_tests, (int)desc.size(), (unsigned)kv.first, threads, 0u, b.stream)) != cudaSuccess)
+            return fail_cuda("server small-test launch", e);
+        s->launches++;
+    }
+    for (size_t i : large) {
+        if ((rc = m2_iterate(s->active[i].ctx, k[i]))) return rc;
+        s->launches += (uint32_t)m2_launches_for(s->active[i].ctx, k[i]);
+    }
+    // wait for the quantum, then account and retire
+    for (auto& kv : small) {
+        const cudaError_t e = cudaStreamSynchronize(s->buckets[kv.first].stream);
+        if (e != cudaSuccess) return fail_cuda("server small-test wait", e);
+    }
+    for (auto& kv : small)
+        for (size_t i : kv.second) s->active[i].ctx->iteration += k[i];
+    std::vector<SrvItem> keep;
+    for (size_t i = 0; i < s->active.size(); ++i) {
+        SrvItem& it = s->active[i];
+        int st = M2_OK;
+        if (it.ctx->path == M2_PATH_LARGE) st = m2_sync(it.ctx);
+        else {
+            int dev = 0;
+            cudaMemcpy(&dev, it.ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+            if (dev) st = M2_ESTATE;
+        }
+        it.done += k[i];
+        s->squarings += k[i];
+        if (st != M2_OK) srv_retire(s, it, st);
+        else if (it.done >= it.total) srv_retire(s, it, M2_OK);
+        else keep.push_back(it);
+    }
+    s->active.swap(keep);
+    return M2_OK;
+}
+
+int m2_srv_poll(m2_server* s, m2_srv_result* out, int max, int* n_out) {
+    if (!s || (!out && max > 0)) return M2_EINVAL;
+    int n = 0;
+    while (n < max && !s->finished.empty()) { out[n++] = s->finished.front(); s->finished.pop_front(); }
+    if (n_out) *n_out = n;
+    return M2_OK;
+}
+
+int m2_srv_stats_get(m2_server* s, m2_srv_stats* st) {
+    if (!s || !st) return M2_EINVAL;
+    st->queued = (uint32_t)s->queue.size();
+    st->active = (uint32_t)s->active.size();
+    st->resident_bytes = s->resident;
+    st->budget_bytes = s->budget;
+    st->squarings = s->squarings;
+    st->completed = s->completed;
+    st->steps = s->steps;
+    st->launches = s->launches;
+    return M2_OK;
+}
+
+void m2_srv_destroy(m2_server* s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    for (auto& it : s->active) if (it.ctx) m2_destroy(it.ctx);
+    for (auto& kv : s->buckets) {
+        if (kv.second.stream) cudaStreamSynchronize(kv.second.stream);
+        cudaFree(kv.second.d_tests);
+        if (kv.second.stream) cudaStreamDestroy(kv.second.stream);
+    }
+    delete s;
 }
 
 }  // extern "C"

@@ -229,6 +229,19 @@ __global__ void __launch_bounds__(256, 2) k_small(const SmallTest* tests, int nt
     }
 }
 
+// Largest dynamic shared memory a CTA of `func` may request on the current
+// device: the opt-in maximum less the kernel's static shared memory.  The
+// kernels' limits are set to this rather than to one plan's size: the
+// attribute belongs to the kernel, and contexts of different sizes share it.
+int dyn_smem_limit(const void* func) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, func) == cudaSuccess) v -= (int)fa.sharedSizeBytes;
+    return v > 0 ? v : 48 * 1024;
+}
+
 int small_threads_for(unsigned int h) {
     unsigned int t = h / 4;
     if (t < 32) t = 32;
@@ -239,7 +252,7 @@ size_t small_smem_bytes(unsigned int h, int threads) { return 24ull * h + 8ull *
 
 cudaError_t launch_small(const SmallTest* d_tests, int ntests, unsigned int h, int threads, unsigned int iters_override, cudaStream_t s) {
     const size_t sm = small_smem_bytes(h, threads);
-    cudaError_t e = cudaFuncSetAttribute(k_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = cudaFuncSetAttribute(k_small, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_limit((const void*)k_small));
     if (e != cudaSuccess) return e;
     k_small<<<ntests, threads, sm, s>>>(d_tests, ntests, h, iters_override, nullptr);
     return cudaGetLastError();
@@ -248,7 +261,7 @@ cudaError_t launch_small(const SmallTest* d_tests, int ntests, unsigned int h, i
 cudaError_t launch_small_persistent(const SmallTest* d_tests, int ntests, unsigned int h, int threads, int* d_queue,
                                     int grid, cudaStream_t s) {
     const size_t sm = small_smem_bytes(h, threads);
-    cudaError_t e = cudaFuncSetAttribute(k_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = cudaFuncSetAttribute(k_small, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_limit((const void*)k_small));
     if (e != cudaSuccess) return e;
     k_small<<<grid, threads, sm, s>>>(d_tests, ntests, h, 0u, d_queue);
     return cudaGetLastError();
@@ -257,7 +270,7 @@ cudaError_t launch_small_persistent(const SmallTest* d_tests, int ntests, unsign
 int small_ctas_per_sm(unsigned int h, int threads) {
     int nb = 0;
     const size_t sm = small_smem_bytes(h, threads);
-    if (cudaFuncSetAttribute(k_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) return 1;
+    if (cudaFuncSetAttribute(k_small, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_limit((const void*)k_small)) != cudaSuccess) return 1;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_small, threads, sm) != cudaSuccess) return 1;
     return nb > 0 ? nb : 1;
 }
@@ -483,11 +496,10 @@ size_t large_smem_rows(const LargePlan& P) { return 24ull * 2 * P.B; }
 
 cudaError_t large_setup(const LargePlan& P) {
     cudaError_t e;
-    const int sc = (int)large_smem_cols(P), sr = (int)large_smem_rows(P);
 #define M2_SET(CC)                                                                                          \
     if (P.C == CC) {                                                                                        \
-        if ((e = cudaFuncSetAttribute(k_cols_fwd<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, sc))) return e; \
-        if ((e = cudaFuncSetAttribute(k_cols_inv<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, sc))) return e; \
+        if ((e = cudaFuncSetAttribute(k_cols_fwd<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_limit((const void*)k_cols_fwd<CC>)))) return e; \
+        if ((e = cudaFuncSetAttribute(k_cols_inv<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_limit((const void*)k_cols_inv<CC>)))) return e; \
         if ((e = cudaFuncSetAttribute(k_cols_fwd<CC>, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e; \
         if ((e = cudaFuncSetAttribute(k_cols_inv<CC>, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e; \
     }
@@ -496,7 +508,7 @@ cudaError_t large_setup(const LargePlan& P) {
     if (rows_rb_supported(P) && (e = rows_rb_setup(P))) return e;
     if (cols_q_supported(P) && (e = cols_q_setup(P))) return e;
     if ((e = cudaFuncSetAttribute(k_rows, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
-    return cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, sr);
+    return cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_limit((const void*)k_rows));
 }
 
 cudaError_t launch_large_stage(const LargePlan& P, const LargeBufs& b, int stage, cudaStream_t s) {

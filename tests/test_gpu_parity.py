@@ -94,3 +94,17 @@ def test_paths_agree(m2, p):
             a.iterate(500)
             b.iterate(500)
             _cmp(a.digits(), b.digits(), f"paths p={p}")
+
+
+def test_contexts_of_different_plans_coexist(m2, oracle_mod):
+    """Kernel launch limits are per kernel, shared by every context: a context
+    created later with a smaller plan must not break an earlier larger one."""
+    with m2.Engine(2976221, 1, path=m2.PATH_LARGE) as big, m2.Engine(756839, 1, path=m2.PATH_LARGE) as small:
+        small.iterate(5)
+        big.iterate(5)
+        o = oracle_mod.Oracle(2976221, 1)
+        o.iterate(5)
+        _cmp(big.digits(), o.digits(), "earlier, larger plan")
+        o2 = oracle_mod.Oracle(756839, 1)
+        o2.iterate(5)
+        _cmp(small.digits(), o2.digits(), "later, smaller plan")
