@@ -255,7 +255,11 @@ def run_gb300(a, dist: Dist) -> dict | None:
         b.build()
     dev = dist.local
     torch.cuda.set_device(dev)
-    stream = torch.cuda.current_stream()
+    # One non-default stream carries the L2 flush, the engine's kernels and the
+    # timing events (handle 0 would be the legacy stream, which the engine
+    # does not run on).
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
     eng = m2.Engine(a.p, m2.MODE_PRP, device=dev, stream=stream.cuda_stream)
     info = eng.info()
     ips = a.iters_per_step

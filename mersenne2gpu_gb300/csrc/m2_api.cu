@@ -17,6 +17,7 @@
 #include <vector>
 #include <chrono>
 #include <deque>
+#include <thread>
 
 using m2::i64;
 using m2::u32;
@@ -51,6 +52,30 @@ int get_twiddles(int device, u64 h, TwTables& out) {
     g_tw[{device, h}] = t;
     out = t;
     return M2_OK;
+}
+
+// ---------------- context memory: one stream-ordered pool per device ----------------
+// Contexts allocate and free on their own stream (cudaMallocFromPoolAsync /
+// cudaFreeAsync), so creating or destroying one never waits for work that other
+// contexts have in flight: the serving engine retires tests while others run.
+// The pool keeps freed blocks for reuse (release threshold: unlimited).
+std::mutex g_pool_mu;
+std::map<int, cudaMemPool_t> g_pool;
+
+cudaMemPool_t ctx_pool(int device) {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    auto it = g_pool.find(device);
+    if (it != g_pool.end()) return it->second;
+    cudaMemPoolProps pp{};
+    pp.allocType = cudaMemAllocationTypePinned;
+    pp.location.type = cudaMemLocationTypeDevice;
+    pp.location.id = device;
+    cudaMemPool_t mp = nullptr;
+    if (cudaMemPoolCreate(&mp, &pp) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    uint64_t keep = ~uint64_t(0);
+    cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &keep);
+    g_pool[device] = mp;
+    return mp;
 }
 
 thread_local char g_last_error[256] = "";
@@ -106,12 +131,17 @@ struct m2_ctx {
     long long* d_carries = nullptr;
     ulonglong2* d_za = nullptr;
     uint2* d_zb = nullptr;
+    // GRAPH_ITERS iterations of the three-pass path captured once and replayed
+    cudaGraphExec_t graph = nullptr;
+    bool graph_failed = false;
 };
 
 namespace {
 
 template <class T> int dalloc(m2_ctx* c, T** p, size_t bytes) {
-    if (cudaMalloc((void**)p, bytes) != cudaSuccess) { cudaGetLastError(); return M2_ENOMEM; }
+    cudaMemPool_t mp = ctx_pool(c->device);
+    if (!mp) return M2_ECUDA;
+    if (cudaMallocFromPoolAsync((void**)p, bytes, mp, c->stream) != cudaSuccess) { cudaGetLastError(); *p = nullptr; return M2_ENOMEM; }
     c->bytes += bytes;
     return M2_OK;
 }
@@ -132,6 +162,41 @@ bool plan_large(const m2::Layout& L, int span, u32 carry_pairs, m2k::LargePlan& 
     if (2 * C < (u32)span + 1 || C > P.B) return false;
     P.C = C; P.G = P.B / C;
     return true;
+}
+
+// Iterations of the three-pass path per graph replay: 3 kernel nodes each.
+constexpr uint32_t GRAPH_ITERS = 50;
+
+// Captures GRAPH_ITERS iterations on the context's stream into an executable
+// graph (once); replays cost one launch instead of 3 * GRAPH_ITERS.  Not done
+// while the caller is capturing the stream itself, or if capture is refused
+// (the legacy default stream): launches are then issued one by one.
+bool ensure_graph(m2_ctx* c) {
+    if (c->graph) return true;
+    if (c->graph_failed) return false;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(c->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        c->graph_failed = true;
+        return false;
+    }
+    cudaError_t e = cudaSuccess;
+    for (uint32_t i = 0; i < GRAPH_ITERS && e == cudaSuccess; ++i) e = m2k::launch_large_iteration(c->plan, c->bufs, c->stream);
+    const cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
+    if (e == cudaSuccess && ee == cudaSuccess && g && cudaGraphInstantiate(&c->graph, g, 0) == cudaSuccess) {
+        cudaGraphDestroy(g);
+        return true;
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    c->graph = nullptr;
+    c->graph_failed = true;
+    return false;
 }
 
 int cuda_err(cudaError_t e) { return e == cudaSuccess ? M2_OK : (e == cudaErrorMemoryAllocation ? M2_ENOMEM : M2_ECUDA); }
@@ -228,9 +293,9 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
         m2_destroy(c.release());
         return rc;
     }
-    cudaError_t e = cudaMemcpy(raw->d_w61, raw->L.w61.data(), n, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(raw->d_w31, raw->L.w31.data(), n, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(raw->d_status, 0, sizeof(int));
+    cudaError_t e = cudaMemcpyAsync(raw->d_w61, raw->L.w61.data(), n, cudaMemcpyHostToDevice, raw->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(raw->d_w31, raw->L.w31.data(), n, cudaMemcpyHostToDevice, raw->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(raw->d_status, 0, sizeof(int), raw->stream);
     if (e != cudaSuccess) { m2_destroy(c.release()); return M2_ECUDA; }
     if (path == M2_PATH_SMALL) {
         raw->threads = m2k::small_threads_for((unsigned)h);
@@ -242,8 +307,11 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
         t.tw4 = raw->tw.tw4; t.tc = raw->tw.tc; t.status = raw->d_status;
         t.p = p; t.iters = 0; t.ln = raw->L.ln; t.mode = mode; t.span = raw->span;
         t.carry_threads = raw->carry_threads;
-        if (cudaMemcpy(raw->d_test, &t, sizeof(t), cudaMemcpyHostToDevice) != cudaSuccess) { m2_destroy(c.release()); return M2_ECUDA; }
         raw->h_test = t;
+        if (cudaMemcpyAsync(raw->d_test, &raw->h_test, sizeof(t), cudaMemcpyHostToDevice, raw->stream) != cudaSuccess) {
+            m2_destroy(c.release());
+            return M2_ECUDA;
+        }
     } else {
         const m2k::LargePlan& P = raw->plan;
         raw->plan.mode = mode;
@@ -270,7 +338,10 @@ int m2_iterate(m2_ctx* c, uint32_t k) {
     if (c->path == M2_PATH_SMALL) {
         e = m2k::launch_small(c->d_test, 1, (unsigned)c->L.h, c->threads, k, c->stream);
     } else {
-        for (uint32_t i = 0; i < k && e == cudaSuccess; ++i) e = m2k::launch_large_iteration(c->plan, c->bufs, c->stream);
+        uint32_t left = k;
+        if (left >= GRAPH_ITERS && ensure_graph(c))
+            for (; left >= GRAPH_ITERS && e == cudaSuccess; left -= GRAPH_ITERS) e = cudaGraphLaunch(c->graph, c->stream);
+        for (; left > 0 && e == cudaSuccess; --left) e = m2k::launch_large_iteration(c->plan, c->bufs, c->stream);
     }
     if (e != cudaSuccess) return fail_cuda("m2_iterate launch", e);
     c->iteration += k;
@@ -346,9 +417,12 @@ int m2_info(m2_ctx* c, m2_info_t* info) {
 void m2_destroy(m2_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
-    if (c->stream) cudaStreamSynchronize(c->stream);
-    cudaFree(c->d_w61); cudaFree(c->d_w31); cudaFree(c->d_status); cudaFree(c->d_digits);
-    cudaFree(c->d_test); cudaFree(c->d_carries); cudaFree(c->d_za); cudaFree(c->d_zb);
+    // stream-ordered frees: they follow the context's queued work and do not
+    // wait for other streams; its stream is released once that work is done
+    void* bufs[] = {c->d_w61, c->d_w31, c->d_status, c->d_digits, c->d_test, c->d_carries, c->d_za, c->d_zb};
+    if (c->stream)
+        for (void* b : bufs) if (b) cudaFreeAsync(b, c->stream);
+    if (c->graph) cudaGraphExecDestroy(c->graph);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -550,6 +624,11 @@ int m2_batch_run(const uint32_t* p, const int* modes, const uint32_t* iters, siz
 }  // extern "C"
 
 // ---------------- serving engine ----------------
+// Lanes run independently: the one-CTA tests of one transform size form one
+// lane (one launch advances all of them), every three-pass test is a lane of
+// its own (its context's stream).  A step starts the next quantum on every idle
+// lane, then waits (bounded) until at least one lane has finished and accounts
+// for it, so a long quantum of a large test never holds back small ones.
 namespace {
 
 struct SrvItem {
@@ -557,15 +636,24 @@ struct SrvItem {
     uint32_t p = 0;
     int mode = 0;
     uint32_t total = 0, done = 0;
+    uint32_t inflight = 0;       // squarings launched and not yet accounted
     m2_ctx* ctx = nullptr;
+    cudaEvent_t ev = nullptr;    // three-pass tests: end of the quantum in flight
     uint64_t bytes = 0;
     double t_submit = 0, t_admit = 0;
 };
 
 struct SrvBucket {
     m2k::SmallTest* d_tests = nullptr;
+    m2k::SmallTest* h_tests = nullptr;   // pinned staging of the descriptors
+    int* d_status = nullptr;             // status word of each member for this launch
+    int* h_status = nullptr;             // pinned copy, read once the launch is done
     size_t cap = 0;
     cudaStream_t stream = nullptr;
+    cudaEvent_t ev = nullptr;
+    std::vector<uint64_t> members;       // keys of the tests in the launch in flight
+    std::vector<uint32_t> ks;
+    bool busy = false;
 };
 
 // device memory a test will hold (digits, weights, status, descriptor; the
@@ -578,6 +666,9 @@ uint64_t srv_estimate(uint32_t p) {
     return b;
 }
 
+// longest a step waits for a lane to finish before reporting M2_ETIMEOUT
+constexpr double SRV_WAIT_LIMIT_S = 600.0;
+
 }  // namespace
 
 struct m2_server {
@@ -585,7 +676,8 @@ struct m2_server {
     uint64_t budget = 0;
     uint32_t quantum = 1000;
     std::deque<SrvItem> queue;
-    std::vector<SrvItem> active;
+    std::map<uint64_t, SrvItem> active;   // key: admission order
+    uint64_t next_key = 0;
     std::deque<m2_srv_result> finished;
     std::map<u64, SrvBucket> buckets;
     uint64_t resident = 0, squarings = 0, completed = 0;
@@ -610,10 +702,124 @@ void srv_retire(m2_server* s, SrvItem& it, int status) {
         m2_destroy(it.ctx);
         it.ctx = nullptr;
     }
+    if (it.ev) { cudaEventDestroy(it.ev); it.ev = nullptr; }
     r.t_done = s->now();
     s->resident -= it.bytes;
     s->completed++;
     s->finished.push_back(r);
+}
+
+int srv_bucket_reserve(SrvBucket& b, size_t need) {
+    cudaError_t e;
+    if (!b.stream && (e = cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return fail_cuda("server stream", e);
+    if (!b.ev && (e = cudaEventCreateWithFlags(&b.ev, cudaEventDisableTiming)) != cudaSuccess)
+        return fail_cuda("server event", e);
+    if (b.cap >= need) return M2_OK;
+    cudaFree(b.d_tests); cudaFree(b.d_status); cudaFreeHost(b.h_tests); cudaFreeHost(b.h_status);
+    b.d_tests = nullptr; b.d_status = nullptr; b.h_tests = nullptr; b.h_status = nullptr;
+    const size_t cap = std::max<size_t>({need, 2 * b.cap, 64});
+    if ((e = cudaMalloc(&b.d_tests, cap * sizeof(m2k::SmallTest))) != cudaSuccess ||
+        (e = cudaMalloc(&b.d_status, cap * sizeof(int))) != cudaSuccess ||
+        (e = cudaMallocHost(&b.h_tests, cap * sizeof(m2k::SmallTest))) != cudaSuccess ||
+        (e = cudaMallocHost(&b.h_status, cap * sizeof(int))) != cudaSuccess) {
+        b.cap = 0;
+        return fail_cuda("server descriptors", e);
+    }
+    b.cap = cap;
+    return M2_OK;
+}
+
+// starts a quantum on every idle lane
+int srv_launch(m2_server* s) {
+    std::map<u64, std::vector<uint64_t>> small;
+    for (auto& kv : s->active) {
+        SrvItem& it = kv.second;
+        if (it.inflight) continue;
+        if (it.ctx->path == M2_PATH_SMALL) {
+            auto b = s->buckets.find(it.ctx->L.h);
+            if (b == s->buckets.end() || !b->second.busy) small[it.ctx->L.h].push_back(kv.first);
+            continue;
+        }
+        const uint32_t k = std::min(s->quantum, it.total - it.done);
+        int rc = m2_iterate(it.ctx, k);
+        if (rc) return rc;
+        cudaError_t e = cudaEventRecord(it.ev, it.ctx->stream);
+        if (e != cudaSuccess) return fail_cuda("server event record", e);
+        it.inflight = k;
+        s->launches += (uint32_t)m2_launches_for(it.ctx, k);
+    }
+    for (auto& kv : small) {
+        SrvBucket& b = s->buckets[kv.first];
+        const size_t cnt = kv.second.size();
+        int rc = srv_bucket_reserve(b, cnt);
+        if (rc) return rc;
+        b.members = kv.second;
+        b.ks.resize(cnt);
+        for (size_t j = 0; j < cnt; ++j) {
+            SrvItem& it = s->active[kv.second[j]];
+            b.ks[j] = std::min(s->quantum, it.total - it.done);
+            m2k::SmallTest t = it.ctx->h_test;
+            t.iters = b.ks[j];
+            t.status = b.d_status + j;
+            b.h_tests[j] = t;
+        }
+        cudaError_t e = cudaMemsetAsync(b.d_status, 0, cnt * sizeof(int), b.stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(b.d_tests, b.h_tests, cnt * sizeof(m2k::SmallTest), cudaMemcpyHostToDevice, b.stream);
+        if (e != cudaSuccess) return fail_cuda("server descriptor upload", e);
+        const int threads = s->active[kv.second[0]].ctx->threads;
+        if ((e = m2k::launch_small(b.d_tests, (int)cnt, (unsigned)kv.first, threads, 0u, b.stream)) != cudaSuccess)
+            return fail_cuda("server small-test launch", e);
+        e = cudaMemcpyAsync(b.h_status, b.d_status, cnt * sizeof(int), cudaMemcpyDeviceToHost, b.stream);
+        if (e == cudaSuccess) e = cudaEventRecord(b.ev, b.stream);
+        if (e != cudaSuccess) return fail_cuda("server status readback", e);
+        for (size_t j = 0; j < cnt; ++j) s->active[kv.second[j]].inflight = b.ks[j];
+        b.busy = true;
+        s->launches++;
+    }
+    return M2_OK;
+}
+
+// accounts for every lane whose quantum has finished; *lanes = how many
+int srv_harvest(m2_server* s, int* lanes, bool* busy_left) {
+    *lanes = 0;
+    *busy_left = false;
+    for (auto& kv : s->buckets) {
+        SrvBucket& b = kv.second;
+        if (!b.busy) continue;
+        const cudaError_t e = cudaEventQuery(b.ev);
+        if (e == cudaErrorNotReady) { *busy_left = true; continue; }
+        if (e != cudaSuccess) return fail_cuda("server small-test wait", e);
+        b.busy = false;
+        ++*lanes;
+        for (size_t j = 0; j < b.members.size(); ++j) {
+            auto f = s->active.find(b.members[j]);
+            SrvItem& it = f->second;
+            const uint32_t k = b.ks[j];
+            it.inflight = 0;
+            it.done += k;
+            it.ctx->iteration += k;
+            s->squarings += k;
+            const int st = b.h_status[j] ? M2_ESTATE : M2_OK;
+            if (st != M2_OK || it.done >= it.total) { srv_retire(s, it, st); s->active.erase(f); }
+        }
+        b.members.clear();
+    }
+    for (auto f = s->active.begin(); f != s->active.end();) {
+        SrvItem& it = f->second;
+        if (it.ctx->path != M2_PATH_LARGE || !it.inflight) { ++f; continue; }
+        const cudaError_t e = cudaEventQuery(it.ev);
+        if (e == cudaErrorNotReady) { *busy_left = true; ++f; continue; }
+        if (e != cudaSuccess) return fail_cuda("server large-test wait", e);
+        ++*lanes;
+        it.done += it.inflight;
+        s->squarings += it.inflight;
+        it.inflight = 0;
+        const int st = m2_sync(it.ctx);
+        if (st != M2_OK || it.done >= it.total) { srv_retire(s, it, st); f = s->active.erase(f); }
+        else ++f;
+    }
+    return M2_OK;
 }
 
 }  // namespace
@@ -660,72 +866,29 @@ int m2_srv_step(m2_server* s) {
         s->resident += it.bytes;
         if (rc != M2_OK) { it.ctx = nullptr; srv_retire(s, it, rc); continue; }
         if (it.total == 0) { srv_retire(s, it, M2_OK); continue; }
-        s->active.push_back(it);
+        if (it.ctx->path == M2_PATH_LARGE) {
+            const cudaError_t e = cudaEventCreateWithFlags(&it.ev, cudaEventDisableTiming);
+            if (e != cudaSuccess) { srv_retire(s, it, fail_cuda("server event", e)); continue; }
+        }
+        s->active.emplace(s->next_key++, it);
     }
     if (s->active.empty()) return M2_OK;
     s->steps++;
-    // one quantum for every active test: small ones batched per transform size
-    std::map<u64, std::vector<size_t>> small;
-    std::vector<size_t> large;
-    for (size_t i = 0; i < s->active.size(); ++i) {
-        if (s->active[i].ctx->path == M2_PATH_SMALL) small[s->active[i].ctx->L.h].push_back(i);
-        else large.push_back(i);
-    }
-    std::vector<uint32_t> k(s->active.size());
-    for (size_t i = 0; i < s->active.size(); ++i) k[i] = std::min(s->quantum, s->active[i].total - s->active[i].done);
-    int rc = M2_OK;
-    for (auto& kv : small) {
-        SrvBucket& b = s->buckets[kv.first];
-        cudaError_t e;
-        if (!b.stream && (e = cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking)) != cudaSuccess)
-            return fail_cuda("server stream", e);
-        if (b.cap < kv.second.size()) {
-            cudaFree(b.d_tests);
-            b.cap = std::max<size_t>(kv.second.size(), 2 * b.cap);
-            if ((e = cudaMalloc(&b.d_tests, b.cap * sizeof(m2k::SmallTest))) != cudaSuccess) { b.cap = 0; return fail_cuda("server descriptors", e); }
+    int rc = srv_launch(s);
+    if (rc) return rc;
+    // wait until a lane finishes (polling; bounded)
+    const auto t_start = std::chrono::steady_clock::now();
+    for (;;) {
+        int lanes = 0;
+        bool busy = false;
+        if ((rc = srv_harvest(s, &lanes, &busy))) return rc;
+        if (lanes > 0 || !busy) return M2_OK;
+        if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() > SRV_WAIT_LIMIT_S) {
+            std::snprintf(g_last_error, sizeof(g_last_error), "m2_srv_step: no lane finished within %.0f s", SRV_WAIT_LIMIT_S);
+            return M2_ETIMEOUT;
         }
-        std::vector<m2k::SmallTest> desc;
-        for (size_t i : kv.second) {
-            m2k::SmallTest t = s->active[i].ctx->h_test;
-            t.iters = k[i];
-            desc.push_back(t);
-        }
-        if ((e = cudaMemcpyAsync(b.d_tests, desc.data(), desc.size() * sizeof(m2k::SmallTest), cudaMemcpyHostToDevice, b.stream)) != cudaSuccess)
-            return fail_cuda("server descriptor upload", e);
-        const int threads = s->active[kv.second[0]].ctx->threads;
-        if ((e = m2k::launch_small(b.d_tests, (int)desc.size(), (unsigned)kv.first, threads, 0u, b.stream)) != cudaSuccess)
-            return fail_cuda("server small-test launch", e);
-        s->launches++;
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
-    for (size_t i : large) {
-        if ((rc = m2_iterate(s->active[i].ctx, k[i]))) return rc;
-        s->launches += (uint32_t)m2_launches_for(s->active[i].ctx, k[i]);
-    }
-    // wait for the quantum, then account and retire
-    for (auto& kv : small) {
-        const cudaError_t e = cudaStreamSynchronize(s->buckets[kv.first].stream);
-        if (e != cudaSuccess) return fail_cuda("server small-test wait", e);
-    }
-    for (auto& kv : small)
-        for (size_t i : kv.second) s->active[i].ctx->iteration += k[i];
-    std::vector<SrvItem> keep;
-    for (size_t i = 0; i < s->active.size(); ++i) {
-        SrvItem& it = s->active[i];
-        int st = M2_OK;
-        if (it.ctx->path == M2_PATH_LARGE) st = m2_sync(it.ctx);
-        else {
-            int dev = 0;
-            cudaMemcpy(&dev, it.ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost);
-            if (dev) st = M2_ESTATE;
-        }
-        it.done += k[i];
-        s->squarings += k[i];
-        if (st != M2_OK) srv_retire(s, it, st);
-        else if (it.done >= it.total) srv_retire(s, it, M2_OK);
-        else keep.push_back(it);
-    }
-    s->active.swap(keep);
-    return M2_OK;
 }
 
 int m2_srv_poll(m2_server* s, m2_srv_result* out, int max, int* n_out) {
@@ -752,11 +915,17 @@ int m2_srv_stats_get(m2_server* s, m2_srv_stats* st) {
 void m2_srv_destroy(m2_server* s) {
     if (!s) return;
     cudaSetDevice(s->device);
-    for (auto& it : s->active) if (it.ctx) m2_destroy(it.ctx);
-    for (auto& kv : s->buckets) {
+    for (auto& kv : s->buckets)
         if (kv.second.stream) cudaStreamSynchronize(kv.second.stream);
-        cudaFree(kv.second.d_tests);
-        if (kv.second.stream) cudaStreamDestroy(kv.second.stream);
+    for (auto& kv : s->active) {
+        if (kv.second.ctx) { m2_sync(kv.second.ctx); m2_destroy(kv.second.ctx); }
+        if (kv.second.ev) cudaEventDestroy(kv.second.ev);
+    }
+    for (auto& kv : s->buckets) {
+        SrvBucket& b = kv.second;
+        cudaFree(b.d_tests); cudaFree(b.d_status); cudaFreeHost(b.h_tests); cudaFreeHost(b.h_status);
+        if (b.ev) cudaEventDestroy(b.ev);
+        if (b.stream) cudaStreamDestroy(b.stream);
     }
     delete s;
 }
