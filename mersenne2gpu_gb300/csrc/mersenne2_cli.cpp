@@ -12,7 +12,8 @@
 //
 // Additions: the mode word prp3 (x <- 3 x^2, the GF61 prototype's PRP), --res64
 // (append the 64-bit residue to every progress line), --path small|large,
-// --checkpoint FILE / --resume FILE (state files, see m2_checkpoint.hpp), and
+// --checkpoint FILE / --resume FILE (state files: magic, p, mode, iteration, n,
+// canonical digits, FNV-1a checksum; written through a temporary file), and
 // a final "res64=" line.
 #include "m2gpu.h"
 
