@@ -315,7 +315,7 @@ def run_gb300(a, dist: Dist) -> dict | None:
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e_value = e2e_s * 1e3 / (a.steps * ips) / dist.world
     h2d = 8 * info.n
-    d2h = 8 * info.n + (8 * info.rows * (info.row_len // info.cols_per_cta) if info.path == m2.PATH_LARGE else 0)
+    d2h = 8 * info.n          # canonical digits, carried on the device (m2_get_digits)
 
     # per-kernel device times for the roofline
     stages = eng.profile(a.profile_iters)

@@ -188,6 +188,23 @@ int m2_measure_mul_peak(int device, double* products_per_s);
  * up the array's device address; make it before any stream capture. */
 int m2_square_noalloc(uint32_t p, int mode, int64_t* digits, uint32_t iters, void* stream);
 
+/* ---------------- full carry propagation ----------------
+ * Replaces the reference's block carry with its serial drain, whose carry out
+ * of the top digit re-enters digit 0 (mersenne2_gpu.cpp:2097-2123, 2922-3004).
+ * Device pointers, on `stream` of the current device; returns when done.
+ * digits: n signed words of exponent p's layout; seg_carries (may be NULL):
+ * n / seg_digits words, carry s entering at digit ((s + 1) seg_digits) mod n
+ * (seg_digits a multiple of 8 dividing n).  out: the n canonical digits of
+ * sum digits_j 2^bitpos_j + sum carry_s 2^bitpos_((s+1) seg) mod 2^p - 1, each
+ * in [0, 2^width_j), the all-ones vector (== M_p) written as zero.  The
+ * propagation is a parallel carry-lookahead whose range covers every state the
+ * engine produces; a state outside it (carries between 8-digit chunks of
+ * 2^width or more) returns M2_ESTATE.  Transforms of n <= 64 digits are
+ * propagated sequentially and accept any input.  m2_get_digits, m2_res64 and
+ * m2_verdict run the same propagation on a context's state. */
+int m2_carry_normalize(uint32_t p, const int64_t* digits, const int64_t* seg_carries, uint32_t seg_digits,
+                       uint64_t* out, void* stream);
+
 /* Digit widths (n bytes) of exponent p, without a device; and log2 n. */
 int m2_layout(uint32_t p, int* ln, uint64_t* n, uint8_t* widths /* may be NULL */);
 

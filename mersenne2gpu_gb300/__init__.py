@@ -25,7 +25,7 @@ EXPORTS = (
     "m2_verdict", "m2_info", "m2_destroy", "m2_layout", "m2_strerror", "m2_batch_run",
     "m2_profile", "m2_launches_for", "m2_measure_mul_peak", "m2_square_noalloc",
     "m2_srv_create", "m2_srv_submit", "m2_srv_step", "m2_srv_poll", "m2_srv_stats_get", "m2_srv_destroy",
-    "m2_last_error",
+    "m2_last_error", "m2_carry_normalize",
 )
 
 
@@ -87,6 +87,7 @@ def _lib() -> ctypes.CDLL:
         L.m2_launches_for.restype = u64
         L.m2_measure_mul_peak.argtypes = [i, ctypes.POINTER(ctypes.c_double)]
         L.m2_square_noalloc.argtypes = [u32, i, vp, u32, vp]
+        L.m2_carry_normalize.argtypes = [u32, vp, vp, u32, vp, vp]
         L.m2_last_error.argtypes = []
         L.m2_last_error.restype = ctypes.c_char_p
         for name in EXPORTS:
@@ -246,3 +247,18 @@ def batch_run(ps, modes=None, iters=None, device: int = 0) -> BatchResult:
     _check(L.m2_batch_run(p.ctypes.data, None if m is None else m.ctypes.data, None if it is None else it.ctypes.data,
                           cnt, res.ctypes.data, pr.ctypes.data, device, ctypes.byref(st)), "m2_batch_run")
     return BatchResult(res, pr.astype(bool), st.seconds, st.squarings, st.launches, st.buckets)
+
+
+def carry_normalize(p: int, digits, carries=None, seg: int = 0, out=None, stream=None):
+    """Full carry propagation on the device (m2_carry_normalize): `digits` (and
+    `carries`) are int64 CUDA tensors of exponent p's layout; returns the n
+    canonical digits as a uint64-valued int64 CUDA tensor (`out` if given)."""
+    import torch
+    L = _lib()
+    n = len(digits)
+    if out is None:
+        out = torch.empty(n, dtype=torch.int64, device=digits.device)
+    s = torch.cuda.current_stream(digits.device).cuda_stream if stream is None else stream
+    _check(L.m2_carry_normalize(p, digits.data_ptr(), None if carries is None else carries.data_ptr(), seg,
+                                out.data_ptr(), s), "m2_carry_normalize")
+    return out

@@ -20,7 +20,7 @@ LIB = os.path.join(PKG, "libm2gpu.so")
 CLI = os.path.join(PKG, "mersenne2")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["m2_kernels.cu", "m2_rows.cu", "m2_cols.cu", "m2_api.cu", "m2_peaks.cu", "m2_noalloc.cu"]
+CU_SOURCES = ["m2_kernels.cu", "m2_rows.cu", "m2_cols.cu", "m2_carry.cu", "m2_api.cu", "m2_peaks.cu", "m2_noalloc.cu"]
 CXX_SOURCES = ["m2_host.cpp"]
 
 

@@ -134,6 +134,9 @@ struct m2_ctx {
     // GRAPH_ITERS iterations of the three-pass path captured once and replayed
     cudaGraphExec_t graph = nullptr;
     bool graph_failed = false;
+    // canonical digits and carry-propagation scratch (allocated on first read)
+    unsigned long long* d_canon = nullptr;
+    void* d_norm = nullptr;
 };
 
 namespace {
@@ -210,25 +213,34 @@ int upload_state(m2_ctx* c, const std::vector<u64>& canon) {
     return cuda_err(e);
 }
 
-int read_canonical(m2_ctx* c, std::vector<u64>& out) {
-    int rc = m2_sync(c);
+// Full carry propagation of the context's state on its stream (m2_carry.cu):
+// canonical digits land in d_canon, the summary flags in the scratch.
+int device_canonical(m2_ctx* c, m2k::NormArgs& a) {
+    int rc;
+    if (!c->d_canon && (rc = dalloc(c, &c->d_canon, c->L.n * sizeof(u64)))) return rc;
+    if (!c->d_norm && (rc = dalloc(c, (char**)&c->d_norm, m2k::norm_scratch_bytes(c->L.n)))) return rc;
+    a = m2k::NormArgs{};
+    a.digits = c->d_digits;
+    a.carries = (c->path == M2_PATH_LARGE) ? c->d_carries : nullptr;
+    a.seg = (c->path == M2_PATH_LARGE) ? 2ull * c->plan.C : 0;
+    a.n = c->L.n; a.p = c->L.p; a.ln = c->L.ln;
+    a.out = c->d_canon;
+    a.status = c->d_status;
+    m2k::norm_bind_scratch(a, c->d_norm);
+    const cudaError_t e = m2k::launch_normalize(a, c->stream);
+    return e == cudaSuccess ? M2_OK : fail_cuda("carry propagation launch", e);
+}
+
+// the first digits (enough for 64 bits) and the summary flags of the canonical state
+int read_head(m2_ctx* c, std::vector<u64>& head, unsigned& flags) {
+    m2k::NormArgs a;
+    int rc = device_canonical(c, a);
     if (rc) return rc;
-    std::vector<i64> d(c->L.n);
-    std::vector<i64> car;
-    cudaError_t e = cudaMemcpy(d.data(), c->d_digits, d.size() * sizeof(i64), cudaMemcpyDeviceToHost);
-    u64 seg = 0;
-    if (e == cudaSuccess && c->path == M2_PATH_LARGE) {
-        car.resize((size_t)c->plan.R * c->plan.G);
-        e = cudaMemcpy(car.data(), c->d_carries, car.size() * sizeof(i64), cudaMemcpyDeviceToHost);
-        seg = 2ull * c->plan.C;
-    }
-    if (e != cudaSuccess) return M2_ECUDA;
-    try {
-        out = m2::canonical_digits(c->L, d, car, seg);
-    } catch (const std::exception&) {
-        return M2_ESTATE;
-    }
-    return M2_OK;
+    head.assign(std::min<u64>(c->L.n, 72), 0);
+    cudaError_t e = cudaMemcpyAsync(head.data(), c->d_canon, head.size() * sizeof(u64), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flags, a.flags, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
+    if (e != cudaSuccess) return fail_cuda("digits read", e);
+    return m2_sync(c);
 }
 
 }  // namespace
@@ -358,46 +370,107 @@ int m2_sync(m2_ctx* c) {
 
 int m2_get_digits(m2_ctx* c, uint64_t* out) {
     if (!c || !out) return M2_EINVAL;
-    std::vector<u64> canon;
-    int rc = read_canonical(c, canon);
+    m2k::NormArgs a;
+    int rc = device_canonical(c, a);
     if (rc) return rc;
-    std::memcpy(out, canon.data(), canon.size() * sizeof(u64));
-    return M2_OK;
+    const cudaError_t e = cudaMemcpyAsync(out, c->d_canon, c->L.n * sizeof(u64), cudaMemcpyDeviceToHost, c->stream);
+    if (e != cudaSuccess) return fail_cuda("digits read", e);
+    return m2_sync(c);
 }
 
 int m2_set_digits(m2_ctx* c, const uint64_t* digits, uint32_t iteration) {
     if (!c || !digits) return M2_EINVAL;
     if (m2_sync(c) == M2_ECUDA) return M2_ECUDA;
-    std::vector<u64> canon;
-    try {
-        canon = m2::canonical_from_unsigned(c->L, digits);
-    } catch (const std::exception&) {
-        return M2_EINVAL;
+    // canonical input (every digit below 2^width): balanced on the device;
+    // anything else is reduced on the host first
+    bool canonical = true;
+    for (u64 j = 0; j < c->L.n && canonical; ++j) canonical = (digits[j] >> c->L.width[j]) == 0;
+    int rc;
+    if (canonical) {
+        if (!c->d_canon && (rc = dalloc(c, &c->d_canon, c->L.n * sizeof(u64)))) return rc;
+        cudaError_t e = cudaMemcpyAsync(c->d_canon, digits, c->L.n * sizeof(u64), cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = m2k::launch_balance(c->d_canon, c->d_digits, c->L.p, c->L.ln, c->L.n, c->stream);
+        if (e == cudaSuccess && c->path == M2_PATH_LARGE)
+            e = cudaMemsetAsync(c->d_carries, 0, sizeof(i64) * (size_t)c->plan.R * c->plan.G, c->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return fail_cuda("state upload", e);
+    } else {
+        std::vector<u64> canon;
+        try {
+            canon = m2::canonical_from_unsigned(c->L, digits);
+        } catch (const std::exception&) {
+            return M2_EINVAL;
+        }
+        if ((rc = upload_state(c, canon))) return rc;
+        cudaMemset(c->d_status, 0, sizeof(int));
     }
-    int rc = upload_state(c, canon);
-    if (rc) return rc;
-    cudaMemset(c->d_status, 0, sizeof(int));
     c->iteration = iteration;
     return M2_OK;
 }
 
 int m2_res64(m2_ctx* c, uint64_t* out) {
     if (!c || !out) return M2_EINVAL;
-    std::vector<u64> canon;
-    int rc = read_canonical(c, canon);
+    std::vector<u64> head;
+    unsigned flags = 0;
+    int rc = read_head(c, head, flags);
     if (rc) return rc;
-    *out = m2::res64_of(c->L, canon);
+    u64 r = 0;
+    for (u64 j = 0; j < head.size() && c->L.bitpos[j] < 64; ++j) r |= head[j] << c->L.bitpos[j];
+    *out = r;
     return M2_OK;
 }
 
 int m2_verdict(m2_ctx* c, int* is_prime) {
     if (!c || !is_prime) return M2_EINVAL;
-    std::vector<u64> canon;
-    int rc = read_canonical(c, canon);
+    std::vector<u64> head;
+    unsigned flags = 0;
+    int rc = read_head(c, head, flags);
     if (rc) return rc;
-    const u64 want = c->mode == M2_MODE_LL ? 0 : (c->mode == M2_MODE_PRP ? 9 : 3);
-    *is_prime = m2::equals_small(c->L, canon, want) ? 1 : 0;
+    u64 want = c->mode == M2_MODE_LL ? 0 : (c->mode == M2_MODE_PRP ? 9 : 3);
+    if (c->L.p < 64) want %= (u64(1) << c->L.p) - 1;
+    const std::vector<u64> w = m2::digits_of_small(c->L, want);
+    // digits from index 8 on are zero when the result was all ones (written as
+    // zero) or when no digit there is nonzero
+    bool same = (flags & 1u) || !(flags & 2u);
+    for (u64 j = 0; j < head.size() && same; ++j) same = (head[j] == w[j]);
+    for (u64 j = head.size(); j < w.size() && same; ++j) same = (w[j] == 0);
+    *is_prime = same ? 1 : 0;
     return M2_OK;
+}
+
+int m2_carry_normalize(uint32_t p, const int64_t* digits, const int64_t* seg_carries, uint32_t seg_digits,
+                       uint64_t* out, void* stream) {
+    if (p < 3 || !digits || !out) return M2_EINVAL;
+    if (m2::transform_log2(p) > 30) return M2_EUNSUPPORTED;
+    const int ln = m2::transform_log2(p);
+    const u64 n = u64(1) << ln;
+    if (seg_carries && (seg_digits == 0 || seg_digits % 8 != 0 || n % seg_digits != 0)) return M2_EINVAL;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return M2_ECUDA;
+    cudaMemPool_t mp = ctx_pool(dev);
+    if (!mp) return M2_ECUDA;
+    cudaStream_t s = (cudaStream_t)stream;
+    void* scratch = nullptr;
+    const size_t sb = m2k::norm_scratch_bytes(n) + 64;
+    cudaError_t e = cudaMallocFromPoolAsync(&scratch, sb, mp, s);
+    if (e != cudaSuccess) return fail_cuda("carry scratch", e);
+    m2k::NormArgs a{};
+    a.digits = reinterpret_cast<const long long*>(digits);
+    a.carries = reinterpret_cast<const long long*>(seg_carries);
+    a.seg = seg_carries ? seg_digits : 0;
+    a.n = n; a.p = p; a.ln = ln;
+    a.out = reinterpret_cast<unsigned long long*>(out);
+    m2k::norm_bind_scratch(a, scratch);
+    a.status = reinterpret_cast<int*>(static_cast<char*>(scratch) + m2k::norm_scratch_bytes(n));
+    int st = 0;
+    e = cudaMemsetAsync(a.status, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = m2k::launch_normalize(a, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, a.status, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaFreeAsync(scratch, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail_cuda("carry propagation", e);
+    return st ? M2_ESTATE : M2_OK;
 }
 
 int m2_info(m2_ctx* c, m2_info_t* info) {
@@ -419,7 +492,8 @@ void m2_destroy(m2_ctx* c) {
     cudaSetDevice(c->device);
     // stream-ordered frees: they follow the context's queued work and do not
     // wait for other streams; its stream is released once that work is done
-    void* bufs[] = {c->d_w61, c->d_w31, c->d_status, c->d_digits, c->d_test, c->d_carries, c->d_za, c->d_zb};
+    void* bufs[] = {c->d_w61, c->d_w31, c->d_status, c->d_digits, c->d_test, c->d_carries, c->d_za, c->d_zb,
+                    c->d_canon, c->d_norm};
     if (c->stream)
         for (void* b : bufs) if (b) cudaFreeAsync(b, c->stream);
     if (c->graph) cudaGraphExecDestroy(c->graph);

@@ -80,4 +80,25 @@ unsigned long long large_stage_bytes(const LargePlan& P, int stage);
 // on every SM: independent chains, returns products per second.
 double measure_wide_mul_rate(int device);
 
+// ---- full carry propagation (m2_carry.cu) ----
+struct NormSum;
+struct NormArgs {
+    const long long* digits;          // n signed digit words
+    const long long* carries;         // pending segment carries (n / seg of them) or null
+    unsigned long long seg;           // digits per segment (a multiple of 8) when carries != null
+    unsigned long long n, p;
+    int ln;
+    unsigned long long* out;          // n canonical digits
+    int* status;                      // |= 2 when the state is outside the propagation's range
+    NormSum* block_sum;               // scratch (norm_bind_scratch)
+    long long* block_cin;
+    unsigned int* flags;              // bit 0: the result was all ones (written as zero); bit 1: a digit >= 8 is nonzero
+};
+size_t norm_scratch_bytes(unsigned long long n);
+void norm_bind_scratch(NormArgs& a, void* scratch);
+cudaError_t launch_normalize(const NormArgs& a, cudaStream_t s);
+// canonical digits -> balanced digits with no pending carries
+cudaError_t launch_balance(const unsigned long long* canon, long long* digits, unsigned long long p, int ln,
+                           unsigned long long n, cudaStream_t s);
+
 }  // namespace m2k
