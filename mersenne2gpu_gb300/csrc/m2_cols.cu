@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(CNT, 2) k_cols_inv_q(LargePlan P, LargeBufs bf
             for (int u = 0; u < 2; ++u) {
                 const u32 cc = 2 * h2 + u;
                 const E v = z.ld(r * CC + cc);
-                const u64 x0 = rotl61(v.a, unrot61f(s61[2 * u], ln1)), x1 = rotl61(v.b, unrot61f(s61[2 * u + 1], ln1));
+                const u64 x0 = rotl61(fold61(v.a), unrot61f(s61[2 * u], ln1)), x1 = rotl61(fold61(v.b), unrot61f(s61[2 * u + 1], ln1));
                 const u32 y0 = rotl31(v.c, unrot31f(s31[2 * u], ln1)), y1 = rotl31(v.d, unrot31f(s31[2 * u + 1], ln1));
                 const u64 j = j0 + 2 * cc;
                 const u64 bp1 = bitpos(p, ln, j + 1), bp2 = bitpos(p, ln, j + 2);

@@ -5,9 +5,12 @@
 // quadratic extension, and 2 has order 61 (resp. 31), so the IBDWT weights
 // 2^(k/n) are powers of two and weighting is a bit rotation.
 //
-// Value convention: every stored coordinate is in [0, P61] (resp. [0, P31]);
-// P itself is an alternative representative of 0.  All helpers accept and
-// return that range.
+// Value convention: a GF(P61) coordinate is any representative in
+// [0, 2^61 + 7] (a 64-bit word at most 8 above P61: one fold of any sum or
+// product lands there, so no helper spends a second fold); a GF(P31)
+// coordinate is in [0, P31].  Twiddles are stored canonical ([0, P61]).
+// Helpers accept and return these ranges unless stated otherwise; rotl61 and
+// the CRT need [0, P61] and get it from full61 / fold61.
 #pragma once
 #include <cstdint>
 
@@ -25,24 +28,28 @@ constexpr u32 P31 = (1u << 31) - 1;
 struct E { u64 a, b; u32 c, d; };   // 24-byte dual element
 
 // ---------------- GF(P61) ----------------
-// fold: t <= 2 P61 + 1  ->  [0, P61]
+// 2 P61 and 4 P61: subtrahend offsets (multiples of P61 above every operand)
+constexpr u64 K2_61 = 2 * P61;
+constexpr u64 K4_61 = 4 * P61;
+// fold: any t < 2^64 -> [0, 2^61 + 7]; t <= 2^61 + 7 -> [0, P61]
 __device__ __forceinline__ u64 fold61(u64 t) { return (t & P61) + (t >> 61); }
 __device__ __forceinline__ u64 add61(u64 a, u64 b) { return fold61(a + b); }
-// P61 - b == P61 ^ b for b <= P61
-__device__ __forceinline__ u64 sub61(u64 a, u64 b) { return fold61(a + (P61 ^ b)); }
-__device__ __forceinline__ u64 neg61(u64 b) { return P61 ^ b; }
+__device__ __forceinline__ u64 sub61(u64 a, u64 b) { return fold61(a + (K2_61 - b)); }
+// [0, 2^61 + 7] -> [0, P61 - 1]: the unique canonical representative
+__device__ __forceinline__ u64 full61(u64 x) { x = fold61(x); return x == P61 ? 0 : x; }
 
-// reduce a 128-bit value x < 2^125 (hi, lo) to [0, P61]
+// reduce a 128-bit value x < 2^124 (hi, lo): x >> 61 < 2^63, so the first sum
+// stays below 2^64, and one fold leaves at most P61 + 5
 __device__ __forceinline__ u64 red61(u64 lo, u64 hi) {
-    u64 s = (lo & P61) + ((hi << 3) | (lo >> 61));   // < 2^61 + 2^64 / 2 ... < 2^64
-    s = (s & P61) + (s >> 61);                          // <= P61 + 7
+    const u64 s = (lo & P61) + ((hi << 3) | (lo >> 61));
     return fold61(s);
 }
 __device__ __forceinline__ u64 mul61(u64 a, u64 b) {
     const u64 lo = a * b, hi = __umul64hi(a, b);
     return red61(lo, hi);
 }
-// x * 2^s for x in [0, P61], s in [0, 60]: a rotation of the 61-bit word
+// x * 2^s for x in [0, P61] (not the full range), s in [0, 60]: a rotation of
+// the 61-bit word
 __device__ __forceinline__ u64 rotl61(u64 x, u32 s) {
     return ((x << s) & P61) | (x >> (61u - s));
 }
@@ -63,12 +70,13 @@ __device__ __forceinline__ u32 rotl31(u32 x, u32 s) {
 
 // ---------------- complex products ----------------
 // (a0 + a1 i)(b0 + b1 i) in GF(P61^2): the real part is accumulated as
-// a0 b0 + (2^122 - 1 - a1 b1), which is a0 b0 - a1 b1 modulo P61 because
-// 2^122 - 1 = (2^61 - 1)(2^61 + 1).
+// a0 b0 + (K - a1 b1) with K = 2^123 - 2 = 2 (2^61 - 1)(2^61 + 1), a multiple
+// of P61 above every product of two coordinates ((2^61 + 7)^2 < 2^122 + 2^65);
+// every sum stays below 2^124, the bound of red61.
 __device__ __forceinline__ void cmul61(u64 a0, u64 a1, u64 b0, u64 b1, u64& r0, u64& r1) {
     const u128 ac = (u128)a0 * b0, bd = (u128)a1 * b1;
     const u128 ad = (u128)a0 * b1, bc = (u128)a1 * b0;
-    const u128 m122 = ((u128)1 << 122) - 1;
+    const u128 m122 = ((u128)1 << 123) - 2;
     const u128 re = ac + (m122 - bd);
     const u128 im = ad + bc;
     r0 = red61((u64)re, (u64)(re >> 64));
@@ -78,7 +86,7 @@ __device__ __forceinline__ void cmul61(u64 a0, u64 a1, u64 b0, u64 b1, u64& r0, 
 __device__ __forceinline__ void cmulconj61(u64 a0, u64 a1, u64 b0, u64 b1, u64& r0, u64& r1) {
     const u128 ac = (u128)a0 * b0, bd = (u128)a1 * b1;
     const u128 ad = (u128)a0 * b1, bc = (u128)a1 * b0;
-    const u128 m122 = ((u128)1 << 122) - 1;
+    const u128 m122 = ((u128)1 << 123) - 2;
     const u128 re = ac + bd;
     const u128 im = bc + (m122 - ad);
     r0 = red61((u64)re, (u64)(re >> 64));
@@ -86,7 +94,7 @@ __device__ __forceinline__ void cmulconj61(u64 a0, u64 a1, u64 b0, u64 b1, u64& 
 }
 __device__ __forceinline__ void csqr61(u64 a0, u64 a1, u64& r0, u64& r1) {
     const u128 aa = (u128)a0 * a0, bb = (u128)a1 * a1, ab = (u128)a0 * a1;
-    const u128 m122 = ((u128)1 << 122) - 1;
+    const u128 m122 = ((u128)1 << 123) - 2;
     const u128 re = aa + (m122 - bb);
     const u128 im = ab << 1;
     r0 = red61((u64)re, (u64)(re >> 64));
@@ -142,19 +150,42 @@ __device__ __forceinline__ E esqr(const E& x) {
 // Forward radix-4 step of the per-block-twiddle transform: the block holds a
 // polynomial mod X^(4m) - c; with r^4 = c the outputs are its residues mod
 // X^m - r, X^m + r, X^m - i r, X^m + i r (bit-reversed order of the roots).
+//
+// The GF(P61) half folds once per output, not once per add: the first layer's
+// sums and differences stay unfolded (below 3 2^61 + 8, differences offset by
+// 2 P61), the second layer offsets its differences by 4 P61 (sums below
+// 7 2^61 + 8 < 2^64) and folds.  The GF(P31) half folds every step (32-bit).
+struct L61 { u64 a, b; };   // unfolded GF(P61^2) intermediate
+__device__ __forceinline__ L61 ladd(u64 xa, u64 xb, u64 ya, u64 yb) { return L61{xa + ya, xb + yb}; }
+__device__ __forceinline__ L61 lsub(u64 xa, u64 xb, u64 ya, u64 yb) { return L61{xa + (K2_61 - ya), xb + (K2_61 - yb)}; }
+__device__ __forceinline__ u64 fadd(u64 x, u64 y) { return fold61(x + y); }
+__device__ __forceinline__ u64 fsub(u64 x, u64 y) { return fold61(x + (K4_61 - y)); }
+
 __device__ __forceinline__ void dif4(E& x0, E& x1, E& x2, E& x3, const E& r1, const E& r2, const E& r3) {
     const E u1 = emul(x1, r1), u2 = emul(x2, r2), u3 = emul(x3, r3);
-    const E v0 = eadd(x0, u2), v1 = eadd(u1, u3), v2 = esub(x0, u2), v3 = esub(u1, u3);
-    x0 = eadd(v0, v1); x1 = esub(v0, v1); x2 = eaddi(v2, v3); x3 = esubi(v2, v3);
+    const L61 v0 = ladd(x0.a, x0.b, u2.a, u2.b), v1 = ladd(u1.a, u1.b, u3.a, u3.b);
+    const L61 v2 = lsub(x0.a, x0.b, u2.a, u2.b), v3 = lsub(u1.a, u1.b, u3.a, u3.b);
+    const u32 c0 = add31(x0.c, u2.c), d0 = add31(x0.d, u2.d), c1 = add31(u1.c, u3.c), d1 = add31(u1.d, u3.d);
+    const u32 c2 = sub31(x0.c, u2.c), d2 = sub31(x0.d, u2.d), c3 = sub31(u1.c, u3.c), d3 = sub31(u1.d, u3.d);
+    x0 = E{fadd(v0.a, v1.a), fadd(v0.b, v1.b), add31(c0, c1), add31(d0, d1)};
+    x1 = E{fsub(v0.a, v1.a), fsub(v0.b, v1.b), sub31(c0, c1), sub31(d0, d1)};
+    x2 = E{fsub(v2.a, v3.b), fadd(v2.b, v3.a), sub31(c2, d3), add31(d2, c3)};   // v2 + i v3
+    x3 = E{fadd(v2.a, v3.b), fsub(v2.b, v3.a), add31(c2, d3), sub31(d2, c3)};   // v2 - i v3
 }
 // Exact inverse of dif4 up to the factor 4.
 __device__ __forceinline__ void dit4(E& x0, E& x1, E& x2, E& x3, const E& r1, const E& r2, const E& r3) {
-    const E v0 = eadd(x0, x1), v1 = esub(x0, x1), v2 = eadd(x2, x3), v3 = esub(x3, x2);
-    const E y0 = eadd(v0, v2);
-    const E y2 = emulconj(esub(v0, v2), r2);
-    const E y1 = emulconj(eaddi(v1, v3), r1);
-    const E y3 = emulconj(esubi(v1, v3), r3);
-    x0 = y0; x1 = y1; x2 = y2; x3 = y3;
+    const L61 v0 = ladd(x0.a, x0.b, x1.a, x1.b), v1 = lsub(x0.a, x0.b, x1.a, x1.b);
+    const L61 v2 = ladd(x2.a, x2.b, x3.a, x3.b), v3 = lsub(x3.a, x3.b, x2.a, x2.b);
+    const u32 c0 = add31(x0.c, x1.c), d0 = add31(x0.d, x1.d), c1 = sub31(x0.c, x1.c), d1 = sub31(x0.d, x1.d);
+    const u32 c2 = add31(x2.c, x3.c), d2 = add31(x2.d, x3.d), c3 = sub31(x3.c, x2.c), d3 = sub31(x3.d, x2.d);
+    const E y0 = E{fadd(v0.a, v2.a), fadd(v0.b, v2.b), add31(c0, c2), add31(d0, d2)};
+    const E s2 = E{fsub(v0.a, v2.a), fsub(v0.b, v2.b), sub31(c0, c2), sub31(d0, d2)};
+    const E s1 = E{fsub(v1.a, v3.b), fadd(v1.b, v3.a), sub31(c1, d3), add31(d1, c3)};   // v1 + i v3
+    const E s3 = E{fadd(v1.a, v3.b), fsub(v1.b, v3.a), add31(c1, d3), sub31(d1, c3)};   // v1 - i v3
+    x0 = y0;
+    x1 = emulconj(s1, r1);
+    x2 = emulconj(s2, r2);
+    x3 = emulconj(s3, r3);
 }
 __device__ __forceinline__ void dif2(E& x0, E& x1, const E& r) {
     const E u1 = emul(x1, r);
@@ -200,10 +231,10 @@ __device__ __forceinline__ u32 canon31(u32 x) { return x == P31 ? 0 : x; }
 // Garner: the signed value z with z == r61 (mod P61), z == r31 (mod P31),
 // |z| < P61 P31 / 2.
 __device__ __forceinline__ i128 crt_signed(u64 r61, u32 r31) {
-    r61 = canon61(r61); r31 = canon31(r31);
-    u64 u = sub61(r61, (u64)r31);
-    u = add61(u, rotl61(canon61(u), 31));                 // u (2^31 + 1) == u / P31 (mod P61)
-    u = canon61(u);
+    r61 = full61(r61); r31 = canon31(r31);
+    u64 u = full61(sub61(r61, (u64)r31));
+    u = add61(u, rotl61(u, 31));                          // u (2^31 + 1) == u / P31 (mod P61)
+    u = full61(u);
     const u128 L = ((u128)u << 31) - u + r31;             // u P31 + r31 < P61 P31
     const u128 M = (u128)P61 * P31;
     return (L > (M >> 1)) ? (i128)L - (i128)M : (i128)L;

@@ -57,7 +57,7 @@ __device__ __forceinline__ u32 unrot31(u32 s, int ln) { const u32 t = (s + (u32)
 // unweight element k (digits 2k, 2k+1) and return the two signed convolution words
 __device__ __forceinline__ void unweigh_crt(const E& v, u64 j, const unsigned char* w61, const unsigned char* w31, int ln,
                                             int mode, i128& z0, i128& z1) {
-    const u64 a = rotl61(v.a, unrot61(w61[j], ln)), b = rotl61(v.b, unrot61(w61[j + 1], ln));
+    const u64 a = rotl61(fold61(v.a), unrot61(w61[j], ln)), b = rotl61(fold61(v.b), unrot61(w61[j + 1], ln));
     const u32 c = rotl31(v.c, unrot31(w31[j], ln)), d = rotl31(v.d, unrot31(w31[j + 1], ln));
     z0 = crt_signed(a, c);
     z1 = crt_signed(b, d);

@@ -77,7 +77,8 @@ __device__ __forceinline__ E dpow(E x, unsigned long long e) {
     return r;
 }
 __device__ __forceinline__ unsigned brev(unsigned i, int bits) { return bits ? (__brev(i) >> (32 - bits)) : 0u; }
-__device__ __forceinline__ void put_tw(m2k::DTw* t, unsigned i, const E& v) { t[i] = m2k::DTw{v.a, v.b, v.c, v.d}; }
+// tables hold canonical coordinates (products leave up to P61 + 5)
+__device__ __forceinline__ void put_tw(m2k::DTw* t, unsigned i, const E& v) { t[i] = m2k::DTw{fold61(v.a), fold61(v.b), v.c, v.d}; }
 
 // Twiddle and weight tables of this engine, rebuilt on the device:
 //   tw4[3(S+j)+a-1] = r^a with r = w_{4S}^{br_S(j)}, tc[j] = w_h^{br_{h/2}(j)},
