@@ -131,6 +131,8 @@ struct m2_ctx {
     long long* d_carries = nullptr;
     ulonglong2* d_za = nullptr;
     uint2* d_zb = nullptr;
+    unsigned* d_flags = nullptr;
+    bool fused = false;        // inverse and next forward column pass as one cooperative launch
     // GRAPH_ITERS iterations of the three-pass path captured once and replayed
     cudaGraphExec_t graph = nullptr;
     bool graph_failed = false;
@@ -171,7 +173,7 @@ bool plan_large(const m2::Layout& L, int span, u32 carry_pairs, m2k::LargePlan& 
 constexpr uint32_t GRAPH_ITERS = 50;
 
 // Captures GRAPH_ITERS iterations on the context's stream into an executable
-// graph (once); replays cost one launch instead of 3 * GRAPH_ITERS.  Not done
+// graph (once); replays cost one launch instead of 2 or 3 per iteration.  Not done
 // while the caller is capturing the stream itself, or if capture is refused
 // (the legacy default stream): launches are then issued one by one.
 bool ensure_graph(m2_ctx* c) {
@@ -189,7 +191,7 @@ bool ensure_graph(m2_ctx* c) {
         return false;
     }
     cudaError_t e = cudaSuccess;
-    for (uint32_t i = 0; i < GRAPH_ITERS && e == cudaSuccess; ++i) e = m2k::launch_large_iteration(c->plan, c->bufs, c->stream);
+    e = m2k::launch_large_run(c->plan, c->bufs, GRAPH_ITERS, c->fused, c->stream);
     const cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
     if (e == cudaSuccess && ee == cudaSuccess && g && cudaGraphInstantiate(&c->graph, g, 0) == cudaSuccess) {
         cudaGraphDestroy(g);
@@ -209,6 +211,7 @@ int upload_state(m2_ctx* c, const std::vector<u64>& canon) {
     cudaError_t e = cudaMemcpyAsync(c->d_digits, bal.data(), bal.size() * sizeof(i64), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess && c->path == M2_PATH_LARGE)
         e = cudaMemsetAsync(c->d_carries, 0, sizeof(i64) * (size_t)c->plan.R * c->plan.G, c->stream);
+    if (e == cudaSuccess && c->d_flags) e = cudaMemsetAsync(c->d_flags, 0, sizeof(unsigned) * c->plan.G, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     return cuda_err(e);
 }
@@ -328,13 +331,15 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
         const m2k::LargePlan& P = raw->plan;
         raw->plan.mode = mode;
         if ((rc = dalloc(raw, &raw->d_carries, sizeof(i64) * (size_t)P.R * P.G)) ||
-            (rc = dalloc(raw, &raw->d_za, sizeof(ulonglong2) * h)) || (rc = dalloc(raw, &raw->d_zb, sizeof(uint2) * h))) {
+            (rc = dalloc(raw, &raw->d_za, sizeof(ulonglong2) * h)) || (rc = dalloc(raw, &raw->d_zb, sizeof(uint2) * h)) ||
+            (rc = dalloc(raw, &raw->d_flags, sizeof(unsigned) * P.G))) {
             m2_destroy(c.release());
             return rc;
         }
         raw->bufs = m2k::LargeBufs{raw->d_digits, raw->d_carries, raw->d_za, raw->d_zb, raw->d_w61, raw->d_w31,
-                                   raw->tw.tw4, raw->tw.tc, raw->d_status};
+                                   raw->tw.tw4, raw->tw.tc, raw->d_status, raw->d_flags};
         if (m2k::large_setup(P) != cudaSuccess) { m2_destroy(c.release()); return M2_EUNSUPPORTED; }
+        raw->fused = m2k::cols_mid_supported(P);
     }
     raw->bytes += raw->tw.bytes;
     if ((rc = upload_state(raw, m2::digits_of_small(raw->L, mode == M2_MODE_LL ? 4 : 3)))) { m2_destroy(c.release()); return rc; }
@@ -353,7 +358,7 @@ int m2_iterate(m2_ctx* c, uint32_t k) {
         uint32_t left = k;
         if (left >= GRAPH_ITERS && ensure_graph(c))
             for (; left >= GRAPH_ITERS && e == cudaSuccess; left -= GRAPH_ITERS) e = cudaGraphLaunch(c->graph, c->stream);
-        for (; left > 0 && e == cudaSuccess; --left) e = m2k::launch_large_iteration(c->plan, c->bufs, c->stream);
+        if (left > 0 && e == cudaSuccess) e = m2k::launch_large_run(c->plan, c->bufs, left, c->fused, c->stream);
     }
     if (e != cudaSuccess) return fail_cuda("m2_iterate launch", e);
     c->iteration += k;
@@ -365,6 +370,7 @@ int m2_sync(m2_ctx* c) {
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return M2_ECUDA;
     int st = 0;
     if (cudaMemcpy(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return M2_ECUDA;
+    if (st & m2k::ST_WAIT_TIMEOUT) return M2_ETIMEOUT;
     return st ? M2_ESTATE : M2_OK;
 }
 
@@ -392,6 +398,7 @@ int m2_set_digits(m2_ctx* c, const uint64_t* digits, uint32_t iteration) {
         if (e == cudaSuccess) e = m2k::launch_balance(c->d_canon, c->d_digits, c->L.p, c->L.ln, c->L.n, c->stream);
         if (e == cudaSuccess && c->path == M2_PATH_LARGE)
             e = cudaMemsetAsync(c->d_carries, 0, sizeof(i64) * (size_t)c->plan.R * c->plan.G, c->stream);
+        if (e == cudaSuccess && c->d_flags) e = cudaMemsetAsync(c->d_flags, 0, sizeof(unsigned) * c->plan.G, c->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess) return fail_cuda("state upload", e);
@@ -493,7 +500,7 @@ void m2_destroy(m2_ctx* c) {
     // stream-ordered frees: they follow the context's queued work and do not
     // wait for other streams; its stream is released once that work is done
     void* bufs[] = {c->d_w61, c->d_w31, c->d_status, c->d_digits, c->d_test, c->d_carries, c->d_za, c->d_zb,
-                    c->d_canon, c->d_norm};
+                    c->d_canon, c->d_norm, c->d_flags};
     if (c->stream)
         for (void* b : bufs) if (b) cudaFreeAsync(b, c->stream);
     if (c->graph) cudaGraphExecDestroy(c->graph);
@@ -504,41 +511,51 @@ void m2_destroy(m2_ctx* c) {
 int m2_profile(m2_ctx* c, uint32_t iters, m2_stage_time* out, int max_stages, int* n_stages) {
     if (!c || !out || max_stages < 1 || iters == 0) return M2_EINVAL;
     if (cudaSetDevice(c->device) != cudaSuccess) return M2_ECUDA;
-    const int ns = (c->path == M2_PATH_SMALL) ? 1 : m2k::LARGE_STAGES;
-    const uint32_t launches = (c->path == M2_PATH_SMALL) ? 1u : iters;
-    std::vector<cudaEvent_t> ev((size_t)launches * ns + 1);
+    // the launch sequence m2_iterate issues for `iters` squarings, one event after each
+    std::vector<int> seq;
+    if (c->path == M2_PATH_SMALL) seq.push_back(-1);
+    else if (c->fused) {
+        seq = {0, 1};
+        for (uint32_t i = 1; i < iters; ++i) { seq.push_back(m2k::STAGE_MID); seq.push_back(1); }
+        seq.push_back(2);
+    } else {
+        for (uint32_t i = 0; i < iters; ++i) for (int st = 0; st < m2k::LARGE_STAGES; ++st) seq.push_back(st);
+    }
+    std::vector<cudaEvent_t> ev(seq.size() + 1);
     for (auto& e : ev) if (cudaEventCreate(&e) != cudaSuccess) return M2_ECUDA;
     cudaError_t err = cudaEventRecord(ev[0], c->stream);
-    for (uint32_t it = 0; it < launches && err == cudaSuccess; ++it) {
-        for (int st = 0; st < ns && err == cudaSuccess; ++st) {
-            if (c->path == M2_PATH_SMALL) err = m2k::launch_small(c->d_test, 1, (unsigned)c->L.h, c->threads, iters, c->stream);
-            else err = m2k::launch_large_stage(c->plan, c->bufs, st, c->stream);
-            if (err == cudaSuccess) err = cudaEventRecord(ev[(size_t)it * ns + st + 1], c->stream);
-        }
+    for (size_t i = 0; i < seq.size() && err == cudaSuccess; ++i) {
+        if (seq[i] < 0) err = m2k::launch_small(c->d_test, 1, (unsigned)c->L.h, c->threads, iters, c->stream);
+        else err = m2k::launch_large_stage(c->plan, c->bufs, seq[i], c->stream);
+        if (err == cudaSuccess) err = cudaEventRecord(ev[i + 1], c->stream);
     }
     if (err == cudaSuccess) err = cudaStreamSynchronize(c->stream);
-    std::vector<double> tot(ns, 0.0);
+    // per stage (in order of first appearance): total time and launches
+    std::vector<int> order;
+    std::map<int, std::pair<double, uint64_t>> tot;
     if (err == cudaSuccess) {
-        for (uint32_t it = 0; it < launches; ++it)
-            for (int st = 0; st < ns; ++st) {
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, ev[(size_t)it * ns + st], ev[(size_t)it * ns + st + 1]);
-                tot[st] += ms;
-            }
+        for (size_t i = 0; i < seq.size(); ++i) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[i], ev[i + 1]);
+            if (!tot.count(seq[i])) order.push_back(seq[i]);
+            tot[seq[i]].first += ms;
+            tot[seq[i]].second += 1;
+        }
     }
     for (auto& e : ev) cudaEventDestroy(e);
-    if (err != cudaSuccess) return M2_ECUDA;
+    if (err != cudaSuccess) return fail_cuda("m2_profile", err);
     c->iteration += iters;
-    const int k = std::min(ns, max_stages);
-    for (int st = 0; st < k; ++st) {
-        m2_stage_time& o = out[st];
+    const int k = std::min((int)order.size(), max_stages);
+    for (int i = 0; i < k; ++i) {
+        const int st = order[i];
+        m2_stage_time& o = out[i];
         std::memset(&o, 0, sizeof(o));
-        const char* nm = (c->path == M2_PATH_SMALL) ? "k_small" : m2k::large_stage_name(st);
+        const char* nm = (st < 0) ? "k_small" : m2k::large_stage_name(st);
         std::strncpy(o.name, nm, sizeof(o.name) - 1);
-        o.launches = launches;
-        o.ms_per_launch = tot[st] / launches;
-        o.iters_per_launch = (c->path == M2_PATH_SMALL) ? iters : 1u;
-        o.bytes_per_launch = (c->path == M2_PATH_SMALL) ? 16ull * c->L.n : m2k::large_stage_bytes(c->plan, st);
+        o.launches = tot[st].second;
+        o.ms_per_launch = tot[st].first / (double)o.launches;
+        o.iters_per_launch = (st < 0) ? iters : 1u;
+        o.bytes_per_launch = (st < 0) ? 16ull * c->L.n : m2k::large_stage_bytes(c->plan, st);
     }
     if (n_stages) *n_stages = k;
     return M2_OK;
@@ -546,7 +563,11 @@ int m2_profile(m2_ctx* c, uint32_t iters, m2_stage_time* out, int max_stages, in
 
 uint64_t m2_launches_for(m2_ctx* c, uint32_t k) {
     if (!c || k == 0) return 0;
-    return (c->path == M2_PATH_SMALL) ? 1ull : (uint64_t)m2k::LARGE_STAGES * k;
+    if (c->path == M2_PATH_SMALL) return 1ull;
+    if (!c->fused) return (uint64_t)m2k::LARGE_STAGES * k;
+    // graph replays of GRAPH_ITERS squarings, then the rest in one sequence
+    const uint64_t chunks = c->graph_failed ? 0 : k / GRAPH_ITERS, rest = k - chunks * GRAPH_ITERS;
+    return chunks * (2ull * GRAPH_ITERS + 1) + (rest ? 2 * rest + 1 : 0);
 }
 
 int m2_measure_mul_peak(int device, double* products_per_s) {

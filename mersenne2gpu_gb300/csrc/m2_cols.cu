@@ -167,26 +167,39 @@ __device__ __forceinline__ void colpass_inv(const S6c& z, u32 base, u32 stride, 
     for (int m = 0; m < 4; ++m) z.st(base + stride * (l + 4 * m), x[m]);
 }
 
-}  // namespace
-
 // element (row r, column c) of the CTA's column group lives at r*CC + c
-__global__ void __launch_bounds__(CNT, 2) k_cols_fwd_q(LargePlan P, LargeBufs bf) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const S6c z = make_s6c(smem, CR * CC);
-    const u32 B = P.B, G = P.G, g = blockIdx.x, tid = threadIdx.x;
+
+// ---- stages shared by the three column kernels ----
+
+// forward row stage: pending carry (the carry out of the segment before this
+// row's segment), fields, weights.  Digits come from global memory, or from
+// the CTA's own shared slots (the fused kernel), where each element slot of a
+// row holds its two digits in the al/ah and bl/bh words.
+template <bool FROM_SMEM>
+__device__ __forceinline__ void fwd_row_stage(const S6c& z, const LargePlan& P, const LargeBufs& bf, u32 g) {
+    const u32 B = P.B, G = P.G, tid = threadIdx.x;
     const u64 RG = (u64)CR * G;
     const u32 p = P.p;
     const int ln = P.ln;
-    // row stage: pending carry, fields, weights
 #pragma unroll 1
     for (u32 r = tid; r < (u32)CR; r += CNT) {
         const u64 s = (u64)r * G + g;
-        i64 c = bf.carries[(s + RG - 1) % RG];
+        const u64 sp = (s + RG - 1) % RG;
+        i64 c = FROM_SMEM ? (i64)__ldcg(reinterpret_cast<const long long*>(bf.carries + sp)) : bf.carries[sp];
         const u64 j0 = 2 * ((u64)r * B + (u64)g * CC);
         i64 d[2 * CC];
-        const longlong2* src = reinterpret_cast<const longlong2*>(bf.digits + j0);
+        if (FROM_SMEM) {
 #pragma unroll
-        for (int u = 0; u < CC; ++u) { const longlong2 v = src[u]; d[2 * u] = v.x; d[2 * u + 1] = v.y; }
+            for (int u = 0; u < CC; ++u) {
+                const u32 q = swzc(r * CC + u);
+                d[2 * u] = (i64)((u64)z.al[q] | ((u64)z.ah[q] << 32));
+                d[2 * u + 1] = (i64)((u64)z.bl[q] | ((u64)z.bh[q] << 32));
+            }
+        } else {
+            const longlong2* src = reinterpret_cast<const longlong2*>(bf.digits + j0);
+#pragma unroll
+            for (int u = 0; u < CC; ++u) { const longlong2 v = src[u]; d[2 * u] = v.x; d[2 * u + 1] = v.y; }
+        }
 #pragma unroll
         for (int u = 0; u < 2 * CC; ++u) {
             if (u < P.span) d[u] = split_balanced64(d[u] + c, width_of(p, ln, j0 + u), c);
@@ -201,8 +214,11 @@ __global__ void __launch_bounds__(CNT, 2) k_cols_fwd_q(LargePlan P, LargeBufs bf
             z.st(r * CC + 2 * h2 + 1, weigh(d[4 * h2 + 2], d[4 * h2 + 3], a.z, a.w, b.z, b.w));
         }
     }
-    __syncthreads();
-    const u32 l = tid & 3u;
+}
+
+// forward passes A, B (shared memory) and C (to global memory)
+__device__ __forceinline__ void fwd_passes(const S6c& z, const LargePlan& P, const LargeBufs& bf, u32 g) {
+    const u32 B = P.B, tid = threadIdx.x, l = tid & 3u;
     // pass A: levels 1-2 (blocks of 1024 and 256 rows)
 #pragma unroll 1
     for (u32 L = tid; L < (u32)(CC * CR / 4); L += CNT) {
@@ -235,13 +251,9 @@ __global__ void __launch_bounds__(CNT, 2) k_cols_fwd_q(LargePlan P, LargeBufs bf
     }
 }
 
-__global__ void __launch_bounds__(CNT, 2) k_cols_inv_q(LargePlan P, LargeBufs bf) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const S6c z = make_s6c(smem, CR * CC);
-    const u32 B = P.B, G = P.G, g = blockIdx.x, tid = threadIdx.x;
-    const u32 p = P.p;
-    const int ln = P.ln;
-    // pass C inverse: level 5, from global memory
+// inverse passes C (from global memory), B and A
+__device__ __forceinline__ void inv_passes(const S6c& z, const LargePlan& P, const LargeBufs& bf, u32 g) {
+    const u32 B = P.B, tid = threadIdx.x, l = tid & 3u;
 #pragma unroll 1
     for (u32 Gq = tid; Gq < (u32)(CC * CR / 4); Gq += CNT) {
         const u32 c = Gq % CC, J = Gq / CC;
@@ -259,7 +271,6 @@ __global__ void __launch_bounds__(CNT, 2) k_cols_inv_q(LargePlan P, LargeBufs bf
         for (int b = 0; b < 4; ++b) z.st((4 * J + b) * CC + c, x[b]);
     }
     __syncthreads();
-    const u32 l = tid & 3u;
 #pragma unroll 1
     for (u32 L = tid; L < (u32)(CC * CR / 4); L += CNT) {
         const u32 sc = L >> 2, c = sc % CC, rest = sc / CC, jb = rest / 4, ib = rest % 4;
@@ -271,8 +282,16 @@ __global__ void __launch_bounds__(CNT, 2) k_cols_inv_q(LargePlan P, LargeBufs bf
         const u32 sc = L >> 2, c = sc % CC, i = sc / CC;
         colpass_inv(z, i * CC + c, (CR / 16) * CC, l, bf.tw4, 1, 0, 0);
     }
-    __syncthreads();
-    // row stage: unweight, CRT, carry within the row segment of 8 digits
+}
+
+// inverse row stage: unweight, CRT, carry within the row segment of 8 digits;
+// the digits go to global memory or back into the row's own shared slots, the
+// segment's carry out to global memory
+template <bool TO_SMEM>
+__device__ __forceinline__ void inv_row_stage(const S6c& z, const LargePlan& P, const LargeBufs& bf, u32 g) {
+    const u32 B = P.B, G = P.G, tid = threadIdx.x;
+    const u32 p = P.p;
+    const int ln = P.ln;
 #pragma unroll 1
     for (u32 r = tid; r < (u32)CR; r += CNT) {
         const u64 e0 = (u64)r * B + (u64)g * CC, j0 = 2 * e0;
@@ -302,12 +321,83 @@ __global__ void __launch_bounds__(CNT, 2) k_cols_inv_q(LargePlan P, LargeBufs bf
                 bp = bp2;
             }
         }
-        longlong2* dst = reinterpret_cast<longlong2*>(bf.digits + j0);
+        if (TO_SMEM) {
 #pragma unroll
-        for (int u = 0; u < CC; ++u) dst[u] = make_longlong2(d[2 * u], d[2 * u + 1]);
-        if (bad) atomicExch(bf.status, ST_CARRY_RANGE);
+            for (int u = 0; u < CC; ++u) {
+                const u32 q = swzc(r * CC + u);
+                z.al[q] = (u32)(u64)d[2 * u]; z.ah[q] = (u32)((u64)d[2 * u] >> 32);
+                z.bl[q] = (u32)(u64)d[2 * u + 1]; z.bh[q] = (u32)((u64)d[2 * u + 1] >> 32);
+            }
+        } else {
+            longlong2* dst = reinterpret_cast<longlong2*>(bf.digits + j0);
+#pragma unroll
+            for (int u = 0; u < CC; ++u) dst[u] = make_longlong2(d[2 * u], d[2 * u + 1]);
+        }
+        if (bad) atomicOr(bf.status, ST_CARRY_RANGE);
         bf.carries[(u64)r * G + g] = c;
     }
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* a) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(unsigned* a, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(a), "r"(v) : "memory");
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(CNT, 2) k_cols_fwd_q(LargePlan P, LargeBufs bf) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const S6c z = make_s6c(smem, CR * CC);
+    fwd_row_stage<false>(z, P, bf, blockIdx.x);
+    __syncthreads();
+    fwd_passes(z, P, bf, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(CNT, 2) k_cols_inv_q(LargePlan P, LargeBufs bf) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const S6c z = make_s6c(smem, CR * CC);
+    inv_passes(z, P, bf, blockIdx.x);
+    __syncthreads();
+    inv_row_stage<false>(z, P, bf, blockIdx.x);
+}
+
+// The inverse column pass of one squaring fused with the forward column pass
+// of the next: the digits never leave the CTA; only the segment carries go
+// through global memory, from CTA g-1 to CTA g (CTA G-1 to CTA 0 for the row
+// before).  Every CTA publishes its carries, raises its flag to this launch's
+// epoch (one more than its value at entry; every launch raises every flag
+// once, so all flags are equal between launches) and waits, bounded, for its
+// predecessor's flag.  Launched cooperatively, so all G CTAs are resident and
+// the waits end; a wait that runs out sets ST_WAIT_TIMEOUT and the CTA goes on.
+__global__ void __launch_bounds__(CNT, 2) k_cols_mid_q(LargePlan P, LargeBufs bf) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ unsigned s_epoch;
+    const S6c z = make_s6c(smem, CR * CC);
+    const u32 g = blockIdx.x, G = P.G;
+    if (threadIdx.x == 0) s_epoch = bf.flags[g] + 1u;
+    inv_passes(z, P, bf, g);
+    __syncthreads();
+    inv_row_stage<true>(z, P, bf, g);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned ep = s_epoch;
+        st_release(bf.flags + g, ep);
+        const unsigned* prev = bf.flags + (g + G - 1) % G;
+        unsigned it = 0;
+        while ((int)(ld_acquire(prev) - ep) < 0) {
+            if (++it > (1u << 20)) { atomicOr(bf.status, ST_WAIT_TIMEOUT); break; }
+            __nanosleep(64);
+        }
+    }
+    __syncthreads();
+    fwd_row_stage<true>(z, P, bf, g);
+    __syncthreads();
+    fwd_passes(z, P, bf, g);
 }
 
 bool cols_q_supported(const LargePlan& P) { return P.R == (u32)CR && P.C == (u32)CC && P.span < 2 * CC; }
@@ -317,8 +407,24 @@ cudaError_t cols_q_setup(const LargePlan& P) {
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_cols_fwd_q, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
     if ((e = cudaFuncSetAttribute(k_cols_inv_q, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
+    if ((e = cudaFuncSetAttribute(k_cols_mid_q, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
     if ((e = cudaFuncSetAttribute(k_cols_fwd_q, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
-    return cudaFuncSetAttribute(k_cols_inv_q, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if ((e = cudaFuncSetAttribute(k_cols_inv_q, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
+    return cudaFuncSetAttribute(k_cols_mid_q, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+}
+
+// true when all G CTAs of the fused kernel fit on the device at once
+bool cols_mid_supported(const LargePlan& P) {
+    if (!cols_q_supported(P)) return false;
+    int dev = 0, sms = 0, per = 0, coop = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return false;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return false;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cols_mid_q, CNT, 24ull * CR * CC) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return (long long)per * sms >= (long long)P.G;
 }
 
 cudaError_t launch_cols_q(const LargePlan& P, const LargeBufs& b, bool inverse, cudaStream_t s) {
@@ -326,6 +432,20 @@ cudaError_t launch_cols_q(const LargePlan& P, const LargeBufs& b, bool inverse, 
     if (inverse) k_cols_inv_q<<<P.G, CNT, sm, s>>>(P, b);
     else k_cols_fwd_q<<<P.G, CNT, sm, s>>>(P, b);
     return cudaGetLastError();
+}
+
+cudaError_t launch_cols_mid(const LargePlan& P, const LargeBufs& b, cudaStream_t s) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(P.G);
+    cfg.blockDim = dim3(CNT);
+    cfg.dynamicSmemBytes = 24ull * CR * CC;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_cols_mid_q, P, b);
 }
 
 }  // namespace m2k

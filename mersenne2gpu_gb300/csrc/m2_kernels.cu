@@ -513,6 +513,7 @@ cudaError_t large_setup(const LargePlan& P) {
 
 cudaError_t launch_large_stage(const LargePlan& P, const LargeBufs& b, int stage, cudaStream_t s) {
     const size_t sc = large_smem_cols(P), sr = large_smem_rows(P);
+    if (stage == STAGE_MID) return launch_cols_mid(P, b, s);
     if (stage != 1 && cols_q_supported(P)) return launch_cols_q(P, b, stage == 2, s);
     if (stage == 0) {
 #define M2_FWD(CC) if (P.C == CC) k_cols_fwd<CC><<<P.G, LTC, sc, s>>>(P, b);
@@ -530,8 +531,8 @@ cudaError_t launch_large_stage(const LargePlan& P, const LargeBufs& b, int stage
 }
 
 const char* large_stage_name(int stage) {
-    static const char* names[] = {"k_cols_fwd", "k_rows", "k_cols_inv"};
-    return (stage >= 0 && stage < 3) ? names[stage] : "?";
+    static const char* names[] = {"k_cols_fwd", "k_rows", "k_cols_inv", "k_cols_mid"};
+    return (stage >= 0 && stage < 4) ? names[stage] : "?";
 }
 
 // Algorithmic bytes of one launch: what the stage must read and write at least.
@@ -540,6 +541,7 @@ unsigned long long large_stage_bytes(const LargePlan& P, int stage) {
     const unsigned long long carries = 8ull * P.R * P.G;
     if (stage == 0) return 16ull * h + carries + 24ull * h;   // digits + carries in, dual elements out
     if (stage == 1) return 48ull * h;                          // dual elements in and out
+    if (stage == STAGE_MID) return 48ull * h + 2 * carries;    // dual elements in and out, carries out and in
     return 24ull * h + 16ull * h + carries;                    // dual elements in, digits + carries out
 }
 
@@ -549,6 +551,19 @@ cudaError_t launch_large_iteration(const LargePlan& P, const LargeBufs& b, cudaS
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+cudaError_t launch_large_run(const LargePlan& P, const LargeBufs& b, unsigned k, bool fused, cudaStream_t s) {
+    cudaError_t e = cudaSuccess;
+    if (k == 0) return e;
+    if (!fused) {
+        for (unsigned i = 0; i < k && e == cudaSuccess; ++i) e = launch_large_iteration(P, b, s);
+        return e;
+    }
+    if ((e = launch_large_stage(P, b, 0, s)) || (e = launch_large_stage(P, b, 1, s))) return e;
+    for (unsigned i = 1; i < k; ++i)
+        if ((e = launch_large_stage(P, b, STAGE_MID, s)) || (e = launch_large_stage(P, b, 1, s))) return e;
+    return launch_large_stage(P, b, 2, s);
 }
 
 }  // namespace m2k

@@ -11,7 +11,7 @@ struct DTw { unsigned long long a, b; unsigned int c, d; };
 enum Mode : int { LL = 0, PRP = 1, PRP3 = 2 };
 
 // Status word written by kernels (0 = ok).
-enum Status : int { ST_OK = 0, ST_CARRY_RANGE = 1, ST_NORMALIZE = 2 };
+enum Status : int { ST_OK = 0, ST_CARRY_RANGE = 1, ST_NORMALIZE = 2, ST_WAIT_TIMEOUT = 4 };
 
 // One independent test for the whole-iteration-in-one-CTA kernel.
 struct SmallTest {
@@ -48,6 +48,7 @@ struct LargeBufs {
     const DTw* tw4;
     const DTw* tc;
     int* status;
+    unsigned int* flags;      // G epoch flags of the fused column kernel (zero-initialised)
 };
 
 size_t small_smem_bytes(unsigned int h, int threads);
@@ -64,6 +65,9 @@ size_t large_smem_rows(const LargePlan& P);
 cudaError_t large_setup(const LargePlan& P);   // sets max dynamic smem attributes
 cudaError_t launch_large_iteration(const LargePlan& P, const LargeBufs& b, cudaStream_t s);
 constexpr int LARGE_STAGES = 3;
+constexpr int STAGE_MID = 3;   // the fused inverse + forward column pass (k_cols_mid_q)
+// k squarings: fwd, rows, (mid, rows) x (k - 1), inv when fused, else k x (fwd, rows, inv)
+cudaError_t launch_large_run(const LargePlan& P, const LargeBufs& b, unsigned k, bool fused, cudaStream_t s);
 // register-blocked row pass (m2_rows.cu), used for row lengths 1024 and 2048
 bool rows_rb_supported(const LargePlan& P);
 cudaError_t rows_rb_setup(const LargePlan& P);
@@ -72,6 +76,8 @@ cudaError_t launch_rows_rb(const LargePlan& P, const LargeBufs& b, cudaStream_t 
 bool cols_q_supported(const LargePlan& P);
 cudaError_t cols_q_setup(const LargePlan& P);
 cudaError_t launch_cols_q(const LargePlan& P, const LargeBufs& b, bool inverse, cudaStream_t s);
+bool cols_mid_supported(const LargePlan& P);   // all G CTAs co-resident (cooperative launch)
+cudaError_t launch_cols_mid(const LargePlan& P, const LargeBufs& b, cudaStream_t s);
 cudaError_t launch_large_stage(const LargePlan& P, const LargeBufs& b, int stage, cudaStream_t s);
 const char* large_stage_name(int stage);
 unsigned long long large_stage_bytes(const LargePlan& P, int stage);
