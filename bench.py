@@ -211,6 +211,41 @@ def run_reference(a, dist: Dist) -> dict | None:
     }
 
 
+# ---------------------------------------------------------------- n = 2^22
+def run_n22(a, stream) -> dict:
+    """Config 3's second exponent: the seeded prime in [73400329, 142606333]
+    (transform n = 2^22), ms/iter device-timed like the headline (L2 flushed
+    between steps), res64 checked against GMP at the golden checkpoints."""
+    import torch
+
+    import mersenne2gpu_gb300 as m2
+    from mersenne2gpu_gb300.workloads import large_n22_exponent
+    p = large_n22_exponent()
+    ips, steps, warm = a.n22_iters, a.n22_steps, 2
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=stream.device)
+    want = {int(k): v for k, v in ((_load_json(GOLDEN_LARGE) or {}).get(str(p), {}).get("prp", {})).items()}
+    with m2.Engine(p, m2.MODE_PRP, device=stream.device.index or 0, stream=stream.cuda_stream) as eng:
+        info = eng.info()
+        for _ in range(warm):
+            flush.zero_()
+            eng.iterate(ips)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for i in range(steps):
+            flush.zero_()
+            evs[i][0].record(stream)
+            eng.iterate(ips)
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        ms = sum(s.elapsed_time(e) for s, e in evs) / (steps * ips)
+        done = (warm + steps) * ips
+        parity = None
+        if done in want:
+            parity = "ok" if f"{eng.res64():016x}" == want[done] else "MISMATCH"
+    return {"p": p, "n": info.n, "ms_per_iter": ms, "iters": steps * ips, "warmup_iters": warm * ips,
+            "plan": {"rows": info.rows, "row_len": info.row_len, "cols_per_cta": info.cols_per_cta},
+            f"res64@{done}": parity}
+
+
 # ---------------------------------------------------------------- batched
 def run_batched(count: int, plain_sample: int) -> dict:
     import mersenne2gpu_gb300 as m2
@@ -370,6 +405,11 @@ def run_gb300(a, dist: Dist) -> dict | None:
         except Exception as ex:  # noqa: BLE001
             out["cpu_baseline"] = {"value": None, "unit": "ms/iter", "cores": 0, "kind": "reference",
                                    "sample": f"unavailable: {ex}"}
+    if a.n22 and dist.world == 1:
+        try:
+            out["n22"] = run_n22(a, stream)
+        except Exception as ex:  # noqa: BLE001
+            out["n22"] = {"error": str(ex)}
     if a.batch:
         try:
             out["batched"] = run_batched(a.batch_count, a.plain_sample)
@@ -396,6 +436,9 @@ def main() -> int:
     ap.add_argument("--profile-iters", type=int, default=50)
     ap.add_argument("--cpu-iters", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-n22", dest="n22", action="store_false")
+    ap.add_argument("--n22-iters", type=int, default=250)
+    ap.add_argument("--n22-steps", type=int, default=2)
     ap.add_argument("--no-batch", dest="batch", action="store_false")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--plain-sample", type=int, default=8)
