@@ -150,7 +150,8 @@ __device__ __forceinline__ void colpass_fwd(const S6c& z, u32 base, u32 stride, 
     E x[4];
 #pragma unroll
     for (int m = 0; m < 4; ++m) x[m] = z.ld(base + stride * (l + 4 * m));
-    { const Tri A = tri(tw4, SA_, JA); dif4(x[0], x[1], x[2], x[3], A.r1, A.r2, A.r3); }
+    if (SA_ == 1) dif4_1(x[0], x[1], x[2], x[3]);   // the first level: root 1
+    else { const Tri A = tri(tw4, SA_, JA); dif4(x[0], x[1], x[2], x[3], A.r1, A.r2, A.r3); }
     quad_transpose(x, l);
     { const Tri Bt = tri(tw4, 4 * SA_, JB0 + l); dif4(x[0], x[1], x[2], x[3], Bt.r1, Bt.r2, Bt.r3); }
 #pragma unroll
@@ -162,7 +163,8 @@ __device__ __forceinline__ void colpass_inv(const S6c& z, u32 base, u32 stride, 
     for (int m = 0; m < 4; ++m) x[m] = z.ld(base + stride * (4 * l + m));
     { const Tri Bt = tri(tw4, 4 * SA_, JB0 + l); dit4(x[0], x[1], x[2], x[3], Bt.r1, Bt.r2, Bt.r3); }
     quad_transpose(x, l);
-    { const Tri A = tri(tw4, SA_, JA); dit4(x[0], x[1], x[2], x[3], A.r1, A.r2, A.r3); }
+    if (SA_ == 1) dit4_1(x[0], x[1], x[2], x[3]);   // the first level: root 1
+    else { const Tri A = tri(tw4, SA_, JA); dit4(x[0], x[1], x[2], x[3], A.r1, A.r2, A.r3); }
 #pragma unroll
     for (int m = 0; m < 4; ++m) z.st(base + stride * (l + 4 * m), x[m]);
 }

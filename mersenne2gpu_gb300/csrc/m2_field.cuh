@@ -187,6 +187,28 @@ __device__ __forceinline__ void dit4(E& x0, E& x1, E& x2, E& x3, const E& r1, co
     x2 = emulconj(s2, r2);
     x3 = emulconj(s3, r3);
 }
+// dif4 / dit4 of the transform's first level (one block, root 1): no products
+__device__ __forceinline__ void dif4_1(E& x0, E& x1, E& x2, E& x3) {
+    const L61 v0 = ladd(x0.a, x0.b, x2.a, x2.b), v1 = ladd(x1.a, x1.b, x3.a, x3.b);
+    const L61 v2 = lsub(x0.a, x0.b, x2.a, x2.b), v3 = lsub(x1.a, x1.b, x3.a, x3.b);
+    const u32 c0 = add31(x0.c, x2.c), d0 = add31(x0.d, x2.d), c1 = add31(x1.c, x3.c), d1 = add31(x1.d, x3.d);
+    const u32 c2 = sub31(x0.c, x2.c), d2 = sub31(x0.d, x2.d), c3 = sub31(x1.c, x3.c), d3 = sub31(x1.d, x3.d);
+    x0 = E{fadd(v0.a, v1.a), fadd(v0.b, v1.b), add31(c0, c1), add31(d0, d1)};
+    x1 = E{fsub(v0.a, v1.a), fsub(v0.b, v1.b), sub31(c0, c1), sub31(d0, d1)};
+    x2 = E{fsub(v2.a, v3.b), fadd(v2.b, v3.a), sub31(c2, d3), add31(d2, c3)};
+    x3 = E{fadd(v2.a, v3.b), fsub(v2.b, v3.a), add31(c2, d3), sub31(d2, c3)};
+}
+__device__ __forceinline__ void dit4_1(E& x0, E& x1, E& x2, E& x3) {
+    const L61 v0 = ladd(x0.a, x0.b, x1.a, x1.b), v1 = lsub(x0.a, x0.b, x1.a, x1.b);
+    const L61 v2 = ladd(x2.a, x2.b, x3.a, x3.b), v3 = lsub(x3.a, x3.b, x2.a, x2.b);
+    const u32 c0 = add31(x0.c, x1.c), d0 = add31(x0.d, x1.d), c1 = sub31(x0.c, x1.c), d1 = sub31(x0.d, x1.d);
+    const u32 c2 = add31(x2.c, x3.c), d2 = add31(x2.d, x3.d), c3 = sub31(x3.c, x2.c), d3 = sub31(x3.d, x2.d);
+    const E y0 = E{fadd(v0.a, v2.a), fadd(v0.b, v2.b), add31(c0, c2), add31(d0, d2)};
+    const E y2 = E{fsub(v0.a, v2.a), fsub(v0.b, v2.b), sub31(c0, c2), sub31(d0, d2)};
+    const E y1 = E{fsub(v1.a, v3.b), fadd(v1.b, v3.a), sub31(c1, d3), add31(d1, c3)};
+    const E y3 = E{fadd(v1.a, v3.b), fsub(v1.b, v3.a), add31(c1, d3), sub31(d1, c3)};
+    x0 = y0; x1 = y1; x2 = y2; x3 = y3;
+}
 __device__ __forceinline__ void dif2(E& x0, E& x1, const E& r) {
     const E u1 = emul(x1, r);
     const E y0 = eadd(x0, u1), y1 = esub(x0, u1);

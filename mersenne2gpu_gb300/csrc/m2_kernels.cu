@@ -99,7 +99,8 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
                 const u32 j = b / Q, i = b % Q, base = j * M + i;
                 E x0 = z.ld(base), x1 = z.ld(base + Q), x2 = z.ld(base + 2 * Q), x3 = z.ld(base + 3 * Q);
                 const u32 ti = 3 * (S + j);
-                dif4(x0, x1, x2, x3, ldtw(T.tw4, ti), ldtw(T.tw4, ti + 1), ldtw(T.tw4, ti + 2));
+                if (S == 1) dif4_1(x0, x1, x2, x3);   // the first level: root 1
+                else dif4(x0, x1, x2, x3, ldtw(T.tw4, ti), ldtw(T.tw4, ti + 1), ldtw(T.tw4, ti + 2));
                 z.st(base, x0); z.st(base + Q, x1); z.st(base + 2 * Q, x2); z.st(base + 3 * Q, x3);
             }
             __syncthreads();
@@ -142,7 +143,8 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
                 const u32 j = b / Q, i = b % Q, base = j * M + i;
                 E x0 = z.ld(base), x1 = z.ld(base + Q), x2 = z.ld(base + 2 * Q), x3 = z.ld(base + 3 * Q);
                 const u32 ti = 3 * (S + j);
-                dit4(x0, x1, x2, x3, ldtw(T.tw4, ti), ldtw(T.tw4, ti + 1), ldtw(T.tw4, ti + 2));
+                if (S == 1) dit4_1(x0, x1, x2, x3);
+                else dit4(x0, x1, x2, x3, ldtw(T.tw4, ti), ldtw(T.tw4, ti + 1), ldtw(T.tw4, ti + 2));
                 z.st(base, x0); z.st(base + Q, x1); z.st(base + 2 * Q, x2); z.st(base + 3 * Q, x3);
             }
             __syncthreads();
@@ -318,7 +320,8 @@ __global__ void __launch_bounds__(LTC, 2) k_cols_fwd(LargePlan P, LargeBufs bf) 
             const u32 i0 = r0 * C + cc, i1 = (r0 + Q) * C + cc, i2 = (r0 + 2 * Q) * C + cc, i3 = (r0 + 3 * Q) * C + cc;
             E x0 = z.ld(i0), x1 = z.ld(i1), x2 = z.ld(i2), x3 = z.ld(i3);
             const u32 ti = 3 * (S + j);
-            dif4(x0, x1, x2, x3, ldtw(bf.tw4, ti), ldtw(bf.tw4, ti + 1), ldtw(bf.tw4, ti + 2));
+            if (S == 1) dif4_1(x0, x1, x2, x3);   // the first level: root 1
+            else dif4(x0, x1, x2, x3, ldtw(bf.tw4, ti), ldtw(bf.tw4, ti + 1), ldtw(bf.tw4, ti + 2));
             z.st(i0, x0); z.st(i1, x1); z.st(i2, x2); z.st(i3, x3);
         }
         __syncthreads();
@@ -464,7 +467,8 @@ __global__ void __launch_bounds__(LTC, 2) k_cols_inv(LargePlan P, LargeBufs bf) 
             const u32 i0 = r0 * C + cc, i1 = (r0 + Q) * C + cc, i2 = (r0 + 2 * Q) * C + cc, i3 = (r0 + 3 * Q) * C + cc;
             E x0 = z.ld(i0), x1 = z.ld(i1), x2 = z.ld(i2), x3 = z.ld(i3);
             const u32 ti = 3 * (S + j);
-            dit4(x0, x1, x2, x3, ldtw(bf.tw4, ti), ldtw(bf.tw4, ti + 1), ldtw(bf.tw4, ti + 2));
+            if (S == 1) dit4_1(x0, x1, x2, x3);
+            else dit4(x0, x1, x2, x3, ldtw(bf.tw4, ti), ldtw(bf.tw4, ti + 1), ldtw(bf.tw4, ti + 2));
             z.st(i0, x0); z.st(i1, x1); z.st(i2, x2); z.st(i3, x3);
         }
         __syncthreads();
