@@ -354,7 +354,8 @@ def run_gb300(a, dist: Dist) -> dict | None:
 
     # per-kernel device times for the roofline
     stages = eng.profile(a.profile_iters)
-    dom = max(stages, key=lambda s: s["ms_per_launch"])
+    # dominant kernel: the largest share of the squarings' device time
+    dom = max(stages, key=lambda s: s["ms_per_launch"] * s["launches"])
     peaks = _load_json(PEAKS) or {}
     hbm = float(peaks.get("hbm_gbs") or 6800.0)
     peak_src = "measured" if peaks.get("hbm_gbs") else "fallback"
@@ -393,7 +394,7 @@ def run_gb300(a, dist: Dist) -> dict | None:
                           "bytes_per_iter": B, "t_hbm_ms": t_hbm, "roofline_ms": max(t_hbm, t_mul),
                           "frac": max(t_hbm, t_mul) / ms_iter_rank,
                           "achieved_products_per_s": W / (ms_iter_rank * 1e-3)},
-        "stages": [{k: s[k] for k in ("name", "ms_per_launch", "bytes_per_launch")} for s in stages],
+        "stages": [{k: s[k] for k in ("name", "ms_per_launch", "launches", "bytes_per_launch")} for s in stages],
         "parity": parity or None,
     }
     if a.cpu_baseline and dist.world == 1:
