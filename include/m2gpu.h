@@ -69,6 +69,7 @@ typedef struct {
     int path;               /* M2_PATH_SMALL or M2_PATH_LARGE */
     uint32_t rows, row_len, cols_per_cta, span;   /* large-path plan */
     uint64_t device_bytes;  /* device memory held by the context */
+    uint32_t fused_cols;    /* 1: the inverse column pass and the next forward one run as one launch */
 } m2_info_t;
 
 /* Replaces main()'s setup (mersenne2_gpu.cpp:3727-4028): exponent -> transform,
@@ -137,7 +138,8 @@ typedef struct {
 } m2_srv_stats;
 
 int m2_srv_create(m2_server** out, int device, uint64_t budget_bytes, uint32_t quantum);
-/* iters = 0 runs the full test (p-2 / p / p-1 squarings) */
+/* iters = 0 runs the full test (p-2 / p / p-1 squarings); a test whose device
+ * memory alone exceeds the budget is refused with M2_ENOMEM */
 int m2_srv_submit(m2_server* s, uint64_t id, uint32_t p, int mode, uint32_t iters);
 /* one scheduling round: admit, advance every active test, retire finished ones */
 int m2_srv_step(m2_server* s);

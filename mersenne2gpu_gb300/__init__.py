@@ -45,7 +45,7 @@ class _Info(ctypes.Structure):
     _fields_ = [("p", ctypes.c_uint32), ("mode", ctypes.c_int), ("ln", ctypes.c_int), ("n", ctypes.c_uint64),
                 ("iteration", ctypes.c_uint32), ("total_iters", ctypes.c_uint32), ("path", ctypes.c_int),
                 ("rows", ctypes.c_uint32), ("row_len", ctypes.c_uint32), ("cols_per_cta", ctypes.c_uint32),
-                ("span", ctypes.c_uint32), ("device_bytes", ctypes.c_uint64)]
+                ("span", ctypes.c_uint32), ("device_bytes", ctypes.c_uint64), ("fused_cols", ctypes.c_uint32)]
 
 
 class _StageTime(ctypes.Structure):
@@ -130,6 +130,7 @@ class Info:
     cols_per_cta: int
     span: int
     device_bytes: int
+    fused_cols: int
 
 
 class Engine:
@@ -168,7 +169,7 @@ class Engine:
         _check(self._L.m2_info(self._h, ctypes.byref(i)), "m2_info")
         self.n = i.n
         return Info(i.p, i.mode, i.ln, i.n, i.iteration, i.total_iters, i.path, i.rows, i.row_len,
-                    i.cols_per_cta, i.span, i.device_bytes)
+                    i.cols_per_cta, i.span, i.device_bytes, i.fused_cols)
 
     def iterate(self, k: int) -> None:
         _check(self._L.m2_iterate(self._h, k), "m2_iterate")

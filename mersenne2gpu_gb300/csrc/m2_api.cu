@@ -491,6 +491,7 @@ int m2_info(m2_ctx* c, m2_info_t* info) {
     if (c->path == M2_PATH_LARGE) { info->rows = c->plan.R; info->row_len = c->plan.B; info->cols_per_cta = c->plan.C; }
     else { info->rows = 1; info->row_len = (uint32_t)c->L.h; info->cols_per_cta = (uint32_t)c->threads; }
     info->device_bytes = c->bytes;
+    info->fused_cols = c->fused ? 1u : 0u;
     return M2_OK;
 }
 
@@ -942,6 +943,7 @@ int m2_srv_submit(m2_server* s, uint64_t id, uint32_t p, int mode, uint32_t iter
     const uint32_t full = total_iters_for(p, mode);
     it.total = iters ? std::min(iters, full) : full;
     it.bytes = srv_estimate(p);
+    if (it.bytes > s->budget) return M2_ENOMEM;   // could never be admitted: refused, not queued
     it.t_submit = s->now();
     s->queue.push_back(it);
     return M2_OK;

@@ -17,6 +17,8 @@
 // a final "res64=" line.
 #include "m2gpu.h"
 
+#include <csignal>
+
 #include <algorithm>
 #include <chrono>
 #include <cctype>
@@ -52,6 +54,12 @@ int fail(int rc, const char* what) {
     std::cerr << what << " failed with error " << rc << " (" << m2_strerror(rc) << ")" << std::endl;
     return 1;
 }
+
+// SIGINT stops the run at the next report point (after that point's
+// checkpoint, when one is being written), as the GF61 prototype's handler does
+// (gf61_ntt_prp_opencl_inplace_nobitrev_fused_powonly_blockcarry.cpp:25-33).
+volatile std::sig_atomic_t g_stop = 0;
+extern "C" void on_sigint(int) { g_stop = 1; }
 
 // ---- state file: magic, p, mode, iteration, n, digits, checksum ----
 constexpr uint64_t kMagic = 0x3247504d324d4752ull;   // "RGM2MPG2"
@@ -223,7 +231,15 @@ int main(int argc, char* argv[]) {
     std::cout << "\n";
     std::cout.unsetf(std::ios::fixed);
     if (debug_plan) {
-        if (large) {
+        if (large && info.fused_cols) {
+            // first squaring: fwd, rows; every further one: mid, rows; after the last: inv
+            const uint32_t gcol = info.row_len / info.cols_per_cta;
+            std::cout << "iter_plan_steps=2 (the first squaring starts with k_cols_fwd, the last ends with k_cols_inv)\n"
+                      << "  [0] k_cols_mid gs=" << gcol * 512 << " ls=512 (cooperative)\n"
+                      << "  [1] k_rows gs=" << (info.rows / 2) * 512 << " ls=512\n"
+                      << "  [pre] k_cols_fwd gs=" << gcol * 512 << " ls=512\n"
+                      << "  [post] k_cols_inv gs=" << gcol * 512 << " ls=512\n";
+        } else if (large) {
             std::cout << "iter_plan_steps=3\n"
                       << "  [0] k_cols_fwd gs=" << (info.row_len / info.cols_per_cta) * 256 << " ls=256\n"
                       << "  [1] k_rows gs=" << (info.rows / 2) * 256 << " ls=256\n"
@@ -281,11 +297,19 @@ int main(int argc, char* argv[]) {
     if (max_iters_override != 0u) std::cout << "benchmark_iters=" << total_iters << "\n";
     uint32_t batch = std::max<uint32_t>(1u, report_every != 0u ? report_every : 1000u);
     if ((rc = report(iter))) { m2_destroy(ctx); return fail(rc, "report"); }
+    std::signal(SIGINT, on_sigint);
     while (iter < total_iters) {
         const uint32_t k = std::min(batch, total_iters - iter);
         if ((rc = m2_iterate(ctx, k))) { m2_destroy(ctx); return fail(rc, "m2_iterate"); }
         iter += k;
         if ((rc = report(iter))) { m2_destroy(ctx); return fail(rc, "report"); }
+        if (g_stop && iter < total_iters) {
+            std::cout << "interrupted at iter " << iter;
+            if (!checkpoint.empty()) std::cout << ", state saved to " << checkpoint;
+            std::cout << "\n" << std::flush;
+            m2_destroy(ctx);
+            return 130;
+        }
     }
     int prime = 0;
     uint64_t r64 = 0;

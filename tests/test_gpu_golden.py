@@ -139,3 +139,34 @@ def test_cli_checkpoint_resume(m2, tmp_path):
         f.write(b"\xff\xff")
     r3 = subprocess.run([exe, "21701", "ll", "--resume", ck], capture_output=True, text=True, timeout=60)
     assert r3.returncode == 1 and "checksum mismatch" in r3.stderr
+
+
+def test_cli_sigint_stops_cleanly_and_resumes(m2, tmp_path):
+    """SIGINT (host-side fault injection, no GPU fault): the run stops at the
+    next report point with its checkpoint written and exit status 130; resuming
+    from the checkpoint reaches the same residue as an uninterrupted run."""
+    import signal
+    import subprocess
+    import time
+    cli = os.path.join(os.path.dirname(m2.__file__), "mersenne2")
+    ck = str(tmp_path / "state.m2")
+    args = [cli, "2976221", "prp", "4000", "-N", "400000", "--checkpoint", ck]
+    pr = subprocess.Popen(args, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    t0 = time.time()
+    while not os.path.exists(ck) and time.time() - t0 < 60:
+        time.sleep(0.05)
+    time.sleep(1.0)
+    pr.send_signal(signal.SIGINT)
+    out, err = pr.communicate(timeout=120)
+    assert pr.returncode == 130, (pr.returncode, out[-500:], err[-500:])
+    assert "interrupted at iter" in out
+    stopped = int(out.split("interrupted at iter ")[1].split(",")[0])
+    assert 0 < stopped < 400000
+    r2 = subprocess.run([cli, "2976221", "prp", "100000", "-N", "400000", "--resume", ck],
+                        capture_output=True, text=True, timeout=300)
+    assert r2.returncode == 0, r2.stderr[-500:]
+    assert f"resumed at iter {stopped}" in r2.stdout
+    r3 = subprocess.run([cli, "2976221", "prp", "100000", "-N", "400000"], capture_output=True, text=True, timeout=300)
+    assert r3.returncode == 0
+    res = [ln for ln in r2.stdout.splitlines() if ln.startswith("res64=")]
+    assert res and res == [ln for ln in r3.stdout.splitlines() if ln.startswith("res64=")]

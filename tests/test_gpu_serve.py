@@ -48,3 +48,20 @@ def test_server_budget_limits_admission(m2):
             if len(got) == 12:
                 break
         assert len(got) == 12 and len({r.res64 for r in got}) == 1
+
+
+def test_server_refuses_a_test_larger_than_the_budget(m2):
+    """A request that could never fit is refused at submit, so it cannot block
+    the FIFO queue behind it."""
+    from mersenne2gpu_gb300.serve import Server
+    with Server(budget_bytes=13_000, quantum=500) as srv:
+        with pytest.raises(m2.M2Error, match=r"\(-2\)"):
+            srv.submit(0, 2976221, 1, 100)           # n = 2^17: megabytes
+        srv.submit(1, 9941, 1, 0)                    # still served
+        got = []
+        for _ in range(1000):
+            srv.step()
+            got += srv.poll()
+            if got:
+                break
+        assert len(got) == 1 and got[0].id == 1 and got[0].is_prime
