@@ -56,13 +56,16 @@ __device__ __forceinline__ u64 rotl61(u64 x, u32 s) {
 
 // ---------------- GF(P31) ----------------
 __device__ __forceinline__ u32 fold31(u32 t) { return (t & P31) + (t >> 31); }
-__device__ __forceinline__ u32 add31(u32 a, u32 b) { return fold31(a + b); }
-__device__ __forceinline__ u32 sub31(u32 a, u32 b) { return fold31(a + (P31 ^ b)); }
+// a + b and a - b for a, b in [0, P31]: the unsigned minimum of the sum and the
+// sum less P31 (the difference and the difference plus P31) is the reduced
+// value -- the wrong candidate has wrapped around to a larger number
+__device__ __forceinline__ u32 add31(u32 a, u32 b) { const u32 s = a + b; return min(s, s - P31); }
+__device__ __forceinline__ u32 sub31(u32 a, u32 b) { const u32 s = a - b; return min(s, s + P31); }
 // reduce x < 2^64 to [0, P31]
 __device__ __forceinline__ u32 red31(u64 x) {
     u64 r = (x & P31) + (x >> 31);             // < 2^34
     u32 s = (u32)((r & P31) + (r >> 31));      // <= P31 + 7
-    return fold31(s);
+    return min(s, s - P31);
 }
 __device__ __forceinline__ u32 rotl31(u32 x, u32 s) {
     return ((x << s) & P31) | (x >> (31u - s));
