@@ -72,51 +72,42 @@ __device__ __forceinline__ u32 rotl31(u32 x, u32 s) {
 }
 
 // ---------------- complex products ----------------
-// (a0 + a1 i)(b0 + b1 i) in GF(P61^2): the real part is accumulated as
-// a0 b0 + (K - a1 b1) with K = 2^123 - 2 = 2 (2^61 - 1)(2^61 + 1), a multiple
-// of P61 above every product of two coordinates ((2^61 + 7)^2 < 2^122 + 2^65);
-// every sum stays below 2^124, the bound of red61.
+// (a0 + a1 i)(b0 + b1 i) in GF(P61^2).  The real part a0 b0 - a1 b1 is formed
+// as a0 b0 + a1 (2 P61 - b1): a 64-bit offset of one factor instead of a
+// 128-bit one of the product (2 P61 lies above every coordinate).  With
+// coordinates up to 2^61 + 7 every sum stays below 3 2^122, within red61's
+// bound of 7 2^122.
 __device__ __forceinline__ void cmul61(u64 a0, u64 a1, u64 b0, u64 b1, u64& r0, u64& r1) {
-    const u128 ac = (u128)a0 * b0, bd = (u128)a1 * b1;
-    const u128 ad = (u128)a0 * b1, bc = (u128)a1 * b0;
-    const u128 m122 = ((u128)1 << 123) - 2;
-    const u128 re = ac + (m122 - bd);
-    const u128 im = ad + bc;
+    const u128 re = (u128)a0 * b0 + (u128)a1 * (K2_61 - b1);
+    const u128 im = (u128)a0 * b1 + (u128)a1 * b0;
     r0 = red61((u64)re, (u64)(re >> 64));
     r1 = red61((u64)im, (u64)(im >> 64));
 }
 // (a0 + a1 i) * conj(b0 + b1 i)
 __device__ __forceinline__ void cmulconj61(u64 a0, u64 a1, u64 b0, u64 b1, u64& r0, u64& r1) {
-    const u128 ac = (u128)a0 * b0, bd = (u128)a1 * b1;
-    const u128 ad = (u128)a0 * b1, bc = (u128)a1 * b0;
-    const u128 m122 = ((u128)1 << 123) - 2;
-    const u128 re = ac + bd;
-    const u128 im = bc + (m122 - ad);
+    const u128 re = (u128)a0 * b0 + (u128)a1 * b1;
+    const u128 im = (u128)a1 * b0 + (u128)a0 * (K2_61 - b1);
     r0 = red61((u64)re, (u64)(re >> 64));
     r1 = red61((u64)im, (u64)(im >> 64));
 }
 __device__ __forceinline__ void csqr61(u64 a0, u64 a1, u64& r0, u64& r1) {
-    const u128 aa = (u128)a0 * a0, bb = (u128)a1 * a1, ab = (u128)a0 * a1;
-    const u128 m122 = ((u128)1 << 123) - 2;
-    const u128 re = aa + (m122 - bb);
-    const u128 im = ab << 1;
+    const u128 re = (u128)a0 * a0 + (u128)a1 * (K2_61 - a1);
+    const u128 im = ((u128)a0 * a1) << 1;
     r0 = red61((u64)re, (u64)(re >> 64));
     r1 = red61((u64)im, (u64)(im >> 64));
 }
-// GF(P31^2): real part a0 b0 + (2^62 - 1 - a1 b1), 2^62 - 1 = (2^31-1)(2^31+1)
+// GF(P31^2): the real part a0 b0 - a1 b1 as a0 b0 + a1 (P31 - b1), a chain of
+// two 32x32->64 multiply-adds below 2^63
 __device__ __forceinline__ void cmul31(u32 a0, u32 a1, u32 b0, u32 b1, u32& r0, u32& r1) {
-    const u64 m62 = (1ull << 62) - 1;
-    r0 = red31((u64)a0 * b0 + (m62 - (u64)a1 * b1));
+    r0 = red31((u64)a0 * b0 + (u64)a1 * (P31 - b1));
     r1 = red31((u64)a0 * b1 + (u64)a1 * b0);
 }
 __device__ __forceinline__ void cmulconj31(u32 a0, u32 a1, u32 b0, u32 b1, u32& r0, u32& r1) {
-    const u64 m62 = (1ull << 62) - 1;
     r0 = red31((u64)a0 * b0 + (u64)a1 * b1);
-    r1 = red31((u64)a1 * b0 + (m62 - (u64)a0 * b1));
+    r1 = red31((u64)a1 * b0 + (u64)a0 * (P31 - b1));
 }
 __device__ __forceinline__ void csqr31(u32 a0, u32 a1, u32& r0, u32& r1) {
-    const u64 m62 = (1ull << 62) - 1;
-    r0 = red31((u64)a0 * a0 + (m62 - (u64)a1 * a1));
+    r0 = red31((u64)a0 * a0 + (u64)a1 * (P31 - a1));
     r1 = red31(((u64)a0 * a1) << 1);
 }
 
