@@ -34,6 +34,11 @@ struct TwTables {
 std::mutex g_tw_mu;
 std::map<std::pair<int, u64>, TwTables> g_tw;
 
+cudaMemPool_t ctx_pool(int device);
+
+// Tables of a new transform size come from the stream-ordered pool on a stream
+// of their own, so building them waits for nothing else running on the device
+// (a cudaMalloc may synchronise the whole device).  Kept until the process ends.
 int get_twiddles(int device, u64 h, TwTables& out) {
     std::lock_guard<std::mutex> lk(g_tw_mu);
     auto it = g_tw.find({device, h});
@@ -41,12 +46,18 @@ int get_twiddles(int device, u64 h, TwTables& out) {
     m2::Twiddles T = m2::make_twiddles(h);
     TwTables t;
     const size_t b4 = T.tw4.size() * sizeof(m2::Dual), bc = T.tc.size() * sizeof(m2::Dual);
-    if (cudaMalloc(&t.tw4, b4) != cudaSuccess) return M2_ENOMEM;
-    if (cudaMalloc(&t.tc, bc) != cudaSuccess) { cudaFree(t.tw4); return M2_ENOMEM; }
-    if (cudaMemcpy(t.tw4, T.tw4.data(), b4, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(t.tc, T.tc.data(), bc, cudaMemcpyHostToDevice) != cudaSuccess) {
-        cudaFree(t.tw4); cudaFree(t.tc);
-        return M2_ECUDA;
+    cudaMemPool_t mp = ctx_pool(device);
+    cudaStream_t s = nullptr;
+    if (!mp || cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) { cudaGetLastError(); return M2_ECUDA; }
+    cudaError_t e = cudaMallocFromPoolAsync((void**)&t.tw4, b4, mp, s);
+    if (e == cudaSuccess) e = cudaMallocFromPoolAsync((void**)&t.tc, bc, mp, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(t.tw4, T.tw4.data(), b4, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(t.tc, T.tc.data(), bc, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? M2_ENOMEM : M2_ECUDA;
     }
     t.bytes = b4 + bc;
     g_tw[{device, h}] = t;
