@@ -277,6 +277,8 @@ def run_batched(count: int, plain_sample: int) -> dict:
         "speedup_vs_plain": (tests_per_s / plain_tests_per_s) if (tests_per_s and plain_tests_per_s) else None,
         "bit_exact_vs_plain": f"{same}/{plain_sample}", "buckets": br.buckets, "launches": br.launches,
         "primes_found": int(br.is_prime.sum()),
+        "tuned_threads_per_bucket": {f"n=2^{ln}": {"threads": t[0], "ns_per_test_squaring": round(t[1], 1)}
+                                     for ln in range(3, 14) if (t := m2.batch_tuned(ln)) is not None},
     }
 
 

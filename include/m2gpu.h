@@ -232,6 +232,12 @@ typedef struct {
 int m2_batch_run(const uint32_t* p, const int* modes, const uint32_t* iters, size_t count,
                  uint64_t* res64_out, int* is_prime_out, int device, m2_batch_stats* stats);
 
+/* Threads per transform that m2_batch_run chose for transform size 2^ln on
+ * `device` (autotuned on the first batch containing that size: every candidate
+ * 32 ... 256 times a sample of the batch's own tests; the carry split follows),
+ * and the measured nanoseconds per test-squaring.  M2_EINVAL if not tuned yet. */
+int m2_batch_tuned(int device, int ln, int* threads, double* ns_per_test_iter);
+
 #ifdef __cplusplus
 }
 #endif

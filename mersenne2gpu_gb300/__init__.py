@@ -25,7 +25,7 @@ EXPORTS = (
     "m2_verdict", "m2_info", "m2_destroy", "m2_layout", "m2_strerror", "m2_batch_run",
     "m2_profile", "m2_launches_for", "m2_measure_mul_peak", "m2_square_noalloc",
     "m2_srv_create", "m2_srv_submit", "m2_srv_step", "m2_srv_poll", "m2_srv_stats_get", "m2_srv_destroy",
-    "m2_last_error", "m2_carry_normalize",
+    "m2_last_error", "m2_carry_normalize", "m2_batch_tuned",
 )
 
 
@@ -88,6 +88,7 @@ def _lib() -> ctypes.CDLL:
         L.m2_measure_mul_peak.argtypes = [i, ctypes.POINTER(ctypes.c_double)]
         L.m2_square_noalloc.argtypes = [u32, i, vp, u32, vp]
         L.m2_carry_normalize.argtypes = [u32, vp, vp, u32, vp, vp]
+        L.m2_batch_tuned.argtypes = [i, i, ctypes.POINTER(i), ctypes.POINTER(ctypes.c_double)]
         L.m2_last_error.argtypes = []
         L.m2_last_error.restype = ctypes.c_char_p
         for name in EXPORTS:
@@ -263,3 +264,10 @@ def carry_normalize(p: int, digits, carries=None, seg: int = 0, out=None, stream
     _check(L.m2_carry_normalize(p, digits.data_ptr(), None if carries is None else carries.data_ptr(), seg,
                                 out.data_ptr(), s), "m2_carry_normalize")
     return out
+
+
+def batch_tuned(ln: int, device: int = 0) -> tuple[int, float] | None:
+    """(threads per transform, ns per test-squaring) m2_batch_run chose for n = 2^ln."""
+    t, ns = ctypes.c_int(), ctypes.c_double()
+    rc = _lib().m2_batch_tuned(device, ln, ctypes.byref(t), ctypes.byref(ns))
+    return (t.value, ns.value) if rc == 0 else None

@@ -590,11 +590,97 @@ int m2_measure_mul_peak(int device, double* products_per_s) {
     return M2_OK;
 }
 
+}  // extern "C"
+
 // ---------------- batched engine ----------------
+namespace {
+
+// Threads per transform of the one-CTA kernel, tuned per (device, h): every
+// candidate (32 ... 256; the segmented carry's split follows from it) runs a
+// GPU-filling sample of the bucket's own tests for TUNE_ITERS squarings on
+// scratch copies of their state, and the highest rate of test-squarings per
+// second wins.  Cached for the process.
+struct Tuned { int threads; double ns_per_test_iter; };
+std::mutex g_tune_mu;
+std::map<std::pair<int, u64>, Tuned> g_tune;
+constexpr u32 TUNE_ITERS = 48;
+
+template <class Item>
+int tune_bucket(int device, u64 h, const std::vector<Item>& items, const std::vector<m2k::SmallTest>& tests,
+                const long long* d_dig, int sms, Tuned& out) {
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find({device, h});
+        if (it != g_tune.end()) { out = it->second; return M2_OK; }
+    }
+    const u64 n = 2 * h;
+    const size_t cap = std::min<size_t>(items.size(), (size_t)std::max(sms, 1) * 8);
+    long long* scratch = nullptr;
+    m2k::SmallTest* d_t = nullptr;
+    int* d_st = nullptr;
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&]() {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (st) cudaStreamDestroy(st);
+        cudaFree(scratch); cudaFree(d_t); cudaFree(d_st);
+    };
+    if (cudaMalloc(&scratch, cap * n * sizeof(i64)) != cudaSuccess || cudaMalloc(&d_t, cap * sizeof(m2k::SmallTest)) != cudaSuccess ||
+        cudaMalloc(&d_st, sizeof(int)) != cudaSuccess || cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        cudaGetLastError();
+        cleanup();
+        return M2_ENOMEM;
+    }
+    Tuned best{m2k::small_threads_for((unsigned)h), 0.0};
+    for (int T = 32; T <= 256; T *= 2) {
+        const int per_sm = m2k::small_ctas_per_sm((unsigned)h, T);
+        const size_t ns = std::min(cap, (size_t)per_sm * (size_t)std::max(sms, 1));
+        std::vector<m2k::SmallTest> d(tests.begin(), tests.begin() + ns);
+        for (size_t t = 0; t < ns; ++t) {
+            d[t].digits = scratch + t * n;
+            d[t].status = d_st;
+            d[t].carry_threads = small_carry_threads(items[t].L, items[t].span, T);
+        }
+        cudaError_t e = cudaMemcpyAsync(scratch, d_dig, ns * n * sizeof(i64), cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_t, d.data(), ns * sizeof(m2k::SmallTest), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = m2k::launch_small(d_t, (int)ns, (unsigned)h, T, 2, st);          // warm-up
+        if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+        if (e == cudaSuccess) e = m2k::launch_small(d_t, (int)ns, (unsigned)h, T, TUNE_ITERS, st);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) { cleanup(); return fail_cuda("batch tuning", e); }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double ns_per = ms * 1e6 / ((double)ns * TUNE_ITERS);
+        if (best.ns_per_test_iter == 0.0 || ns_per < best.ns_per_test_iter) best = Tuned{T, ns_per};
+    }
+    cleanup();
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[{device, h}] = best;
+    out = best;
+    return M2_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int m2_batch_tuned(int device, int ln, int* threads, double* ns_per_test_iter) {
+    if (ln < 3 || ln > 14) return M2_EINVAL;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find({device, u64(1) << (ln - 1)});
+    if (it == g_tune.end()) return M2_EINVAL;
+    if (threads) *threads = it->second.threads;
+    if (ns_per_test_iter) *ns_per_test_iter = it->second.ns_per_test_iter;
+    return M2_OK;
+}
+
 // Tests are bucketed by transform length h; every bucket is one persistent
-// launch (CTAs pull test indices from a device counter, longest tests first),
-// all buckets run concurrently on their own streams, and the whole set of
-// launches is captured into one CUDA graph.
+// launch (CTAs pull test indices from a device counter, longest tests first)
+// with its tuned threads per transform, all buckets run concurrently on their
+// own streams, and the whole set of launches is captured into one CUDA graph.
 int m2_batch_run(const uint32_t* p, const int* modes, const uint32_t* iters, size_t count,
                  uint64_t* res64_out, int* is_prime_out, int device, m2_batch_stats* stats) {
     if (!p || count == 0) return M2_EINVAL;
@@ -648,7 +734,7 @@ int m2_batch_run(const uint32_t* p, const int* modes, const uint32_t* iters, siz
         if ((rc = dmal((void**)&d_dig, nt * n * sizeof(i64))) || (rc = dmal((void**)&d_w, nt * n * 2)) ||
             (rc = dmal((void**)&d_tests, nt * sizeof(m2k::SmallTest))) || (rc = dmal((void**)&d_q, 2 * sizeof(int))))
             return rc;
-        const int threads = m2k::small_threads_for((unsigned)h);
+        int threads = m2k::small_threads_for((unsigned)h);
         std::vector<i64> dig(nt * n);
         std::vector<unsigned char> w(nt * n * 2);
         std::vector<m2k::SmallTest> tests(nt);
@@ -666,8 +752,13 @@ int m2_batch_run(const uint32_t* p, const int* modes, const uint32_t* iters, siz
             squarings += it.iters;
         }
         if (cudaMemcpy(d_dig, dig.data(), dig.size() * sizeof(i64), cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(d_w, w.data(), w.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(d_tests, tests.data(), tests.size() * sizeof(m2k::SmallTest), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(d_w, w.data(), w.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            return M2_ECUDA;
+        Tuned tn;
+        if ((rc = tune_bucket(device, h, items, tests, d_dig, sms, tn))) return rc;
+        threads = tn.threads;
+        for (size_t t = 0; t < nt; ++t) tests[t].carry_threads = small_carry_threads(items[t].L, items[t].span, threads);
+        if (cudaMemcpy(d_tests, tests.data(), tests.size() * sizeof(m2k::SmallTest), cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemset(d_q, 0, 2 * sizeof(int)) != cudaSuccess)
             return M2_ECUDA;
         const int per_sm = m2k::small_ctas_per_sm((unsigned)h, threads);

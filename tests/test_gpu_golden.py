@@ -94,6 +94,10 @@ def test_config4_batched_golden_and_plain(m2):
     br = m2.batch_run(ps, iters=iters)
     for i, p in enumerate(ps):
         assert f"{int(br.res64[i]):016x}" == g["res64"][str(p)], p
+    # every bucket was autotuned (threads per transform, 32 ... 256)
+    for ln in sorted({m2.layout(p)[0] for p in ps}):
+        t = m2.batch_tuned(ln)
+        assert t is not None and t[0] in (32, 64, 128, 256) and t[1] > 0, (ln, t)
     # full runs: batched == plain on a spread of exponents (each bucket)
     pick = sorted(set(ps))[:: max(1, len(set(ps)) // 24)]
     full = m2.batch_run(pick)
