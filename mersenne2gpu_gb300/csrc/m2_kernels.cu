@@ -38,6 +38,24 @@ __device__ __forceinline__ SE make_se(unsigned char* base, u32 ne) {
     return SE{(u64*)base, (u64*)base + ne, (u32*)(base + 16ull * ne), (u32*)(base + 16ull * ne) + ne};
 }
 
+// The one-CTA kernel's arrays are indexed through an XOR swizzle of the low
+// four element-index bits by bits 4 and up (one IMAD, three ALU ops): chosen
+// by a bank-conflict model of every access of the kernel (contiguous, radix-4
+// strides 1 ... h/4, radix-2 pairs, centre mirrors, the segmented carry's lane
+// stride n / (2 Tc)) for h = 64 ... 8192 and 32 ... 256 threads, which it
+// leaves with 3.5% of the unswizzled layout's extra shared-memory wavefronts.
+__device__ __forceinline__ u32 swsm(u32 i) { return i ^ ((((i >> 4) * 5u) ^ (i >> 8)) & 15u); }
+struct SZ {
+    u64* a; u64* b; u32* c; u32* d;
+    __device__ __forceinline__ E ld(u32 i) const { const u32 q = swsm(i); return E{a[q], b[q], c[q], d[q]}; }
+    __device__ __forceinline__ void st(u32 i, const E& e) const { const u32 q = swsm(i); a[q] = e.a; b[q] = e.b; c[q] = e.c; d[q] = e.d; }
+    __device__ __forceinline__ u64& A(u32 i) const { return a[swsm(i)]; }
+    __device__ __forceinline__ u64& Bv(u32 i) const { return b[swsm(i)]; }
+};
+__device__ __forceinline__ SZ make_sz(unsigned char* base, u32 ne) {
+    return SZ{(u64*)base, (u64*)base + ne, (u32*)(base + 16ull * ne), (u32*)(base + 16ull * ne) + ne};
+}
+
 __device__ __forceinline__ E ldtw(const DTw* t, u32 i) {
     const u64* q = reinterpret_cast<const u64*>(t + i);
     const u64 a = __ldg(q), b = __ldg(q + 1), cd = __ldg(q + 2);
@@ -72,7 +90,7 @@ __device__ __forceinline__ bool fits64(i128 c) { const i128 hi = c >> 63; return
 // k_small: whole test in one CTA
 // =====================================================================
 __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, unsigned char* smem) {
-    const SE z = make_se(smem, h);
+    const SZ z = make_sz(smem, h);
     i64* cx = reinterpret_cast<i64*>(smem + 24ull * h);
     const u32 tid = threadIdx.x, nt = blockDim.x;
     const u64 n = 2ull * h;
@@ -83,12 +101,12 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
     u32 s4max = 0;
     for (u32 S = 1; 4 * S <= h; S *= 4) s4max = S;
 
-    for (u32 k = tid; k < h; k += nt) { z.a[k] = (u64)T.digits[2 * k]; z.b[k] = (u64)T.digits[2 * k + 1]; }
+    for (u32 k = tid; k < h; k += nt) { z.A(k) = (u64)T.digits[2 * k]; z.Bv(k) = (u64)T.digits[2 * k + 1]; }
     __syncthreads();
 
     for (u32 it = 0; it < iters; ++it) {
         for (u32 k = tid; k < h; k += nt) {
-            const i64 d0 = (i64)z.a[k], d1 = (i64)z.b[k];
+            const i64 d0 = (i64)z.A(k), d1 = (i64)z.Bv(k);
             z.st(k, weigh(d0, d1, T.w61[2 * k], T.w61[2 * k + 1], T.w31[2 * k], T.w31[2 * k + 1]));
         }
         __syncthreads();
@@ -162,12 +180,12 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
                     if (T.mode == LL && k == 0) z0 -= 2;
                     const i64 d0 = split_balanced(z0 + c, width_of(p, ln, 2ull * k), c);
                     const i64 d1 = split_balanced(z1 + c, width_of(p, ln, 2ull * k + 1), c);
-                    z.a[k] = (u64)d0; z.b[k] = (u64)d1;
+                    z.A(k) = (u64)d0; z.Bv(k) = (u64)d1;
                 }
                 int pass = 0;
                 while (c != 0 && pass < 8) {
                     for (u64 j = 0; j < n && c != 0; ++j) {
-                        u64* slot = (j & 1) ? &z.b[j >> 1] : &z.a[j >> 1];
+                        u64* slot = (j & 1) ? &z.Bv((u32)(j >> 1)) : &z.A((u32)(j >> 1));
                         *slot = (u64)split_balanced((i128)(i64)*slot + c, width_of(p, ln, j), c);
                     }
                     ++pass;
@@ -187,7 +205,7 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
                     if (T.mode == LL && k == 0) z0 -= 2;
                     const i64 d0 = split_balanced(z0 + c, width_of(p, ln, 2ull * k), c);
                     const i64 d1 = split_balanced(z1 + c, width_of(p, ln, 2ull * k + 1), c);
-                    z.a[k] = (u64)d0; z.b[k] = (u64)d1;
+                    z.A(k) = (u64)d0; z.Bv(k) = (u64)d1;
                 }
                 if (!fits64(c)) atomicExch(T.status, ST_CARRY_RANGE);
                 cx[tid] = (i64)c;
@@ -198,7 +216,7 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
                 const u64 j0 = (u64)tid * D;
                 for (int u = 0; u <= T.span; ++u) {
                     const u64 j = j0 + (u64)u;
-                    u64* slot = (j & 1) ? &z.b[j >> 1] : &z.a[j >> 1];
+                    u64* slot = (j & 1) ? &z.Bv((u32)(j >> 1)) : &z.A((u32)(j >> 1));
                     if (u < T.span) *slot = (u64)split_balanced64((i64)*slot + c, width_of(p, ln, j), c);
                     else *slot = (u64)((i64)*slot + c);
                 }
@@ -206,7 +224,7 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
             __syncthreads();
         }
     }
-    for (u32 k = tid; k < h; k += nt) { T.digits[2 * k] = (i64)z.a[k]; T.digits[2 * k + 1] = (i64)z.b[k]; }
+    for (u32 k = tid; k < h; k += nt) { T.digits[2 * k] = (i64)z.A(k); T.digits[2 * k + 1] = (i64)z.Bv(k); }
 }
 
 // One CTA per test (queue == nullptr), or a persistent grid whose CTAs take
