@@ -284,6 +284,7 @@ def run_batched(count: int, plain_sample: int) -> dict:
 
 # ---------------------------------------------------------------- main arm
 def run_gb300(a, dist: Dist) -> dict | None:
+    import numpy as np
     import torch
 
     import mersenne2gpu_gb300 as m2
@@ -337,16 +338,18 @@ def run_gb300(a, dist: Dist) -> dict | None:
     ms_iter_rank = dev_ms / (a.steps * ips)
     value = ms_iter_rank / dist.world
 
-    # e2e: through the C ABI with host buffers
-    host = eng.digits()
+    # e2e: through the C ABI with host buffers in pinned memory (digits in,
+    # squarings, canonical digits out; both copies inside the timed region)
+    pinned = torch.empty(info.n, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+    eng.digits(out=pinned)
     it = eng.info().iteration
     torch.cuda.synchronize()
     dist.barrier()
     t0 = time.perf_counter()
     for i in range(a.steps):
-        eng.set_digits(host, it)
+        eng.set_digits(pinned, it)
         eng.iterate(ips)
-        host = eng.digits()
+        eng.digits(out=pinned)
         it += ips
     dist.barrier()
     e2e_s = dist.max(time.perf_counter() - t0)

@@ -178,8 +178,13 @@ class Engine:
     def sync(self) -> None:
         _check(self._L.m2_sync(self._h), "m2_sync")
 
-    def digits(self) -> np.ndarray:
-        out = np.zeros(self.n, dtype=np.uint64)
+    def digits(self, out: np.ndarray | None = None) -> np.ndarray:
+        """Canonical digits; `out` (n uint64, contiguous, e.g. a view of pinned
+        host memory, which the copy then reaches by DMA) is filled if given."""
+        if out is None:
+            out = np.zeros(self.n, dtype=np.uint64)
+        elif out.dtype != np.uint64 or out.shape != (self.n,) or not out.flags.c_contiguous:
+            raise ValueError(f"expected a contiguous uint64 array of {self.n} digits")
         _check(self._L.m2_get_digits(self._h, out.ctypes.data), "m2_get_digits")
         return out
 

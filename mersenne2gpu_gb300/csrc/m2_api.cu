@@ -398,22 +398,25 @@ int m2_get_digits(m2_ctx* c, uint64_t* out) {
 int m2_set_digits(m2_ctx* c, const uint64_t* digits, uint32_t iteration) {
     if (!c || !digits) return M2_EINVAL;
     if (m2_sync(c) == M2_ECUDA) return M2_ECUDA;
-    // canonical input (every digit below 2^width): balanced on the device;
-    // anything else is reduced on the host first
-    bool canonical = true;
-    for (u64 j = 0; j < c->L.n && canonical; ++j) canonical = (digits[j] >> c->L.width[j]) == 0;
+    // canonical input (every digit below 2^width), the usual case: uploaded and
+    // balanced on the device, which also checks that it is canonical; anything
+    // else is reduced on the host first
     int rc;
-    if (canonical) {
-        if (!c->d_canon && (rc = dalloc(c, &c->d_canon, c->L.n * sizeof(u64)))) return rc;
-        cudaError_t e = cudaMemcpyAsync(c->d_canon, digits, c->L.n * sizeof(u64), cudaMemcpyHostToDevice, c->stream);
-        if (e == cudaSuccess) e = m2k::launch_balance(c->d_canon, c->d_digits, c->L.p, c->L.ln, c->L.n, c->stream);
-        if (e == cudaSuccess && c->path == M2_PATH_LARGE)
-            e = cudaMemsetAsync(c->d_carries, 0, sizeof(i64) * (size_t)c->plan.R * c->plan.G, c->stream);
-        if (e == cudaSuccess && c->d_flags) e = cudaMemsetAsync(c->d_flags, 0, sizeof(unsigned) * c->plan.G, c->stream);
-        if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-        if (e != cudaSuccess) return fail_cuda("state upload", e);
-    } else {
+    if (!c->d_canon && (rc = dalloc(c, &c->d_canon, c->L.n * sizeof(u64)))) return rc;
+    if (!c->d_norm && (rc = dalloc(c, (char**)&c->d_norm, m2k::norm_scratch_bytes(c->L.n)))) return rc;
+    unsigned* d_bad = reinterpret_cast<unsigned*>(c->d_norm);   // scratch word, free between reads
+    unsigned bad = 0;
+    cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(unsigned), c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_canon, digits, c->L.n * sizeof(u64), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = m2k::launch_balance(c->d_canon, c->d_digits, c->L.p, c->L.ln, c->L.n, d_bad, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && c->path == M2_PATH_LARGE)
+        e = cudaMemsetAsync(c->d_carries, 0, sizeof(i64) * (size_t)c->plan.R * c->plan.G, c->stream);
+    if (e == cudaSuccess && c->d_flags) e = cudaMemsetAsync(c->d_flags, 0, sizeof(unsigned) * c->plan.G, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return fail_cuda("state upload", e);
+    if (bad) {
         std::vector<u64> canon;
         try {
             canon = m2::canonical_from_unsigned(c->L, digits);

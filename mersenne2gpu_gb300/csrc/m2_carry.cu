@@ -297,17 +297,22 @@ __global__ void k_norm_tiny(NormArgs a) {
 // canonical digits (each < 2^w) -> balanced relaxed digits with no pending
 // carries: a digit >= 2^(w-1) gives 2^w back and a carry of one to the next
 // digit (the top digit's to digit 0): every result lies in [-2^(w-1), 2^(w-1)].
-__global__ void k_balance(const u64* canon, i64* digits, u64 p, int ln, u64 n) {
+// A digit at or above 2^w (not canonical) sets *bad; the caller then loads
+// the state another way (the digits written here are not used).
+__global__ void k_balance(const u64* canon, i64* digits, u64 p, int ln, u64 n, unsigned* bad) {
+    unsigned any = 0;
     for (u64 j = (u64)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (u64)gridDim.x * blockDim.x) {
         const u64 b0 = bitpos(p, ln, j), b1 = bitpos(p, ln, j + 1);
         const u32 w = (u32)(b1 - b0);
         const u64 jp = (j == 0) ? n - 1 : j - 1;
         const u32 wprev = (u32)(bitpos(p, ln, jp + 1) - bitpos(p, ln, jp));
         i64 v = (i64)canon[j];
+        any |= (u32)((canon[j] >> w) != 0);   // widths stay below 64
         if (w > 0 && canon[j] >= (1ull << (w - 1))) v -= (i64)1 << w;
         if (wprev > 0 && canon[jp] >= (1ull << (wprev - 1))) v += 1;
         digits[j] = v;
     }
+    if (bad && __syncthreads_or(any) && threadIdx.x == 0) atomicOr(bad, 1u);
 }
 
 }  // namespace
@@ -342,9 +347,9 @@ cudaError_t launch_normalize(const NormArgs& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_balance(const u64* canon, i64* digits, u64 p, int ln, u64 n, cudaStream_t s) {
+cudaError_t launch_balance(const u64* canon, i64* digits, u64 p, int ln, u64 n, unsigned* bad, cudaStream_t s) {
     const unsigned g = (unsigned)((n + 255) / 256 < 2048 ? (n + 255) / 256 : 2048);
-    k_balance<<<g, 256, 0, s>>>(canon, digits, p, ln, n);
+    k_balance<<<g, 256, 0, s>>>(canon, digits, p, ln, n, bad);
     return cudaGetLastError();
 }
 

@@ -103,8 +103,9 @@ struct NormArgs {
 size_t norm_scratch_bytes(unsigned long long n);
 void norm_bind_scratch(NormArgs& a, void* scratch);
 cudaError_t launch_normalize(const NormArgs& a, cudaStream_t s);
-// canonical digits -> balanced digits with no pending carries
+// canonical digits -> balanced digits with no pending carries; *bad |= 1 when
+// an input digit is not canonical (bad may be null)
 cudaError_t launch_balance(const unsigned long long* canon, long long* digits, unsigned long long p, int ln,
-                           unsigned long long n, cudaStream_t s);
+                           unsigned long long n, unsigned int* bad, cudaStream_t s);
 
 }  // namespace m2k
