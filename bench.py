@@ -23,7 +23,8 @@ Also reported:
             [1000, 18874367], continuous batching under an HBM budget for a
             fixed window: p50/p99 time-to-result per transform size,
             squarings/s, completed results re-run alone
-  parity    res64 at iterations 1000 and 10000 against GMP golden values
+  parity    res64 at iterations 1000 and 21000 (n = 2^21) and 10000 (n = 2^22)
+            against GMP golden values
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 """
@@ -433,7 +434,7 @@ def run_gb300(a, dist: Dist) -> dict | None:
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=7)
+    ap.add_argument("--steps", type=int, default=18)   # 3 + 18 steps of 1000: the state ends at GMP's iteration 21000
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--p", type=int, default=DEFAULT_P)
@@ -443,7 +444,7 @@ def main() -> int:
     ap.add_argument("--cpu-iters", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-n22", dest="n22", action="store_false")
-    ap.add_argument("--n22-iters", type=int, default=250)
+    ap.add_argument("--n22-iters", type=int, default=2500)   # 4 x 2500: checked at GMP's iteration 10000
     ap.add_argument("--n22-steps", type=int, default=2)
     ap.add_argument("--no-batch", dest="batch", action="store_false")
     ap.add_argument("--batch-count", type=int, default=4096)
