@@ -171,8 +171,9 @@ bool plan_large(const m2::Layout& L, int span, u32 carry_pairs, m2k::LargePlan& 
     P.ln = L.ln; P.L = Lh; P.L1 = L1; P.L2 = L2;
     P.R = 1u << L1; P.B = 1u << L2;
     P.span = span; P.p = L.p;
-    u32 C = 16;
-    while (C > 4 && 24ull * C * P.R > 100 * 1024) C >>= 1;
+    // columns per CTA: 4 (more CTAs for the small grids of mid-size transforms),
+    // 8 for the 256 x 2048 plan (n = 2^20), where it measured fastest
+    u32 C = (P.R == 256 && P.B == 2048) ? 8 : 4;
     if (carry_pairs >= 4 && carry_pairs <= 16 && (carry_pairs & (carry_pairs - 1)) == 0) C = carry_pairs;
     while (2 * C < (u32)span + 1 && C < 16) C <<= 1;
     if (2 * C < (u32)span + 1 || C > P.B) return false;
@@ -301,7 +302,9 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
     c->span = m2::carry_span(c->L);
     const u64 h = c->L.h;
     int path = o.path;
-    if (path == M2_PATH_AUTO) path = (h <= 8192) ? M2_PATH_SMALL : M2_PATH_LARGE;
+    // a lone test of h >= 2048 runs faster on the three-pass path's many CTAs
+    // than in one CTA (the one-CTA path pays off when many tests share a launch)
+    if (path == M2_PATH_AUTO) path = (h <= 1024) ? M2_PATH_SMALL : M2_PATH_LARGE;
     if (path == M2_PATH_SMALL && h > 8192) return M2_EUNSUPPORTED;
     if (path == M2_PATH_LARGE && !plan_large(c->L, c->span, o.carry_pairs, c->plan)) return M2_EUNSUPPORTED;
     c->path = path;
@@ -1063,6 +1066,8 @@ int m2_srv_step(m2_server* s) {
         s->queue.pop_front();
         m2_opts o{};
         o.device = s->device;
+        // up to h = 8192 a test joins its size's shared one-CTA launch
+        o.path = (m2::transform_log2(it.p) <= 14) ? M2_PATH_SMALL : M2_PATH_LARGE;
         const int rc = m2_create(&it.ctx, it.p, it.mode, &o);
         it.t_admit = s->now();
         s->resident += it.bytes;
