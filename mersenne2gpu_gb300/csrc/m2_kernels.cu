@@ -10,9 +10,12 @@
 //
 // Two execution shapes:
 //  * k_small: one CTA owns one whole test (state in shared memory) and loops
-//    over iterations on-chip.  Used for n <= 16384 and by the batched engine
-//    (one CTA per test, many tests per launch).
-//  * three-pass path for large n, h = R x B elements:
+//    over iterations on-chip.  Used for a lone test up to n = 2048, and by the
+//    batched engine and the server up to n = 16384 (one CTA per test, many
+//    tests per launch).
+//  * three-pass path, h = R x B elements (these generic kernels serve every
+//    plan; m2_cols.cu and m2_rows.cu hold faster ones for R = 1024 / B = 1024,
+//    2048 and the fused inverse + forward column pass):
 //      k_cols_fwd: apply pending segment carries, weight, first log2 R levels
 //                  down the columns (C adjacent columns per CTA)
 //      k_rows:     last log2 B levels, centre square, first inverse levels on a
@@ -527,7 +530,7 @@ cudaError_t large_setup(const LargePlan& P) {
     }
     M2_FOR_C(M2_SET)
 #undef M2_SET
-    if (rows_rb_supported(P) && (e = rows_rb_setup(P))) return e;
+    if (rows_q_supported(P) && (e = rows_q_setup(P))) return e;
     if (cols_q_supported(P) && (e = cols_q_setup(P))) return e;
     if ((e = cudaFuncSetAttribute(k_rows, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
     return cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_limit((const void*)k_rows));
@@ -542,7 +545,7 @@ cudaError_t launch_large_stage(const LargePlan& P, const LargeBufs& b, int stage
         M2_FOR_C(M2_FWD)
 #undef M2_FWD
     } else if (stage == 1) {
-        if (rows_rb_supported(P)) return launch_rows_rb(P, b, s);
+        if (rows_q_supported(P)) return launch_rows_q(P, b, s);
         k_rows<<<P.R / 2, LT, sr, s>>>(P, b);
     } else {
 #define M2_INV(CC) if (P.C == CC) k_cols_inv<CC><<<P.G, LTC, sc, s>>>(P, b);

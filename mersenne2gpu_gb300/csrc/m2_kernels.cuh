@@ -68,10 +68,10 @@ constexpr int LARGE_STAGES = 3;
 constexpr int STAGE_MID = 3;   // the fused inverse + forward column pass (k_cols_mid_q)
 // k squarings: fwd, rows, (mid, rows) x (k - 1), inv when fused, else k x (fwd, rows, inv)
 cudaError_t launch_large_run(const LargePlan& P, const LargeBufs& b, unsigned k, bool fused, cudaStream_t s);
-// register-blocked row pass (m2_rows.cu), used for row lengths 1024 and 2048
-bool rows_rb_supported(const LargePlan& P);
-cudaError_t rows_rb_setup(const LargePlan& P);
-cudaError_t launch_rows_rb(const LargePlan& P, const LargeBufs& b, cudaStream_t s);
+// quad-shuffle row pass (m2_rows.cu), used for row lengths 1024 and 2048
+bool rows_q_supported(const LargePlan& P);
+cudaError_t rows_q_setup(const LargePlan& P);
+cudaError_t launch_rows_q(const LargePlan& P, const LargeBufs& b, cudaStream_t s);
 // quad-shuffle column passes (m2_cols.cu), used for R = 1024 rows and C = 4
 bool cols_q_supported(const LargePlan& P);
 cudaError_t cols_q_setup(const LargePlan& P);

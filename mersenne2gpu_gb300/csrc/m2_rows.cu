@@ -345,9 +345,9 @@ __global__ void __launch_bounds__(512, (B == 1024) ? 2 : 1) k_rows_q(LargePlan P
     }
 }
 
-bool rows_rb_supported(const LargePlan& P) { return P.B == 1024 || P.B == 2048; }
+bool rows_q_supported(const LargePlan& P) { return P.B == 1024 || P.B == 2048; }
 
-cudaError_t rows_rb_setup(const LargePlan& P) {
+cudaError_t rows_q_setup(const LargePlan& P) {
     const int sm = (int)(24ull * 2 * P.B);
     cudaError_t e;
     if (P.B == 1024) {
@@ -361,7 +361,7 @@ cudaError_t rows_rb_setup(const LargePlan& P) {
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_rows_rb(const LargePlan& P, const LargeBufs& b, cudaStream_t s) {
+cudaError_t launch_rows_q(const LargePlan& P, const LargeBufs& b, cudaStream_t s) {
     const size_t sm = 24ull * 2 * P.B;
     if (P.B == 1024) k_rows_q<1024><<<P.R / 2, 512, sm, s>>>(P, b);
     else if (P.B == 2048) k_rows_q<2048><<<P.R / 2, 512, sm, s>>>(P, b);
