@@ -36,6 +36,14 @@ enum { M2_MODE_LL = 0, M2_MODE_PRP = 1, M2_MODE_PRP3 = 2 };
 /* execution path selection (0 = automatic) */
 enum { M2_PATH_AUTO = 0, M2_PATH_SMALL = 1, M2_PATH_LARGE = 2 };
 
+/* fields of the transform: GF(P61^2) x GF(P31^2) recombined by CRT (the
+ * reference engine, default), or GF(P61^2) alone with the GF61 prototype's
+ * size rule ln + 2((p >> ln) + 1) < 61
+ * (gf61_ntt_prp_opencl_inplace_nobitrev_fused.cpp:124-132): up to twice the
+ * digits, of up to half the width.  GF(P61^2)-only runs on the one-CTA path (n <= 16384,
+ * p < 376832); results are the same residues, in that layout's digits. */
+enum { M2_FIELDS_DUAL = 0, M2_FIELDS_GF61 = 1 };
+
 enum {
     M2_OK = 0,
     M2_EINVAL = -1,       /* bad argument (reference: usage error, exit 1, mersenne2_gpu.cpp:3618-3716) */
@@ -57,6 +65,7 @@ typedef struct {
     uint32_t carry_pairs;   /* -B: carry segment length hint in digit pairs (0 = auto) */
     int path;               /* M2_PATH_* */
     void* stream;           /* cudaStream_t to run on (NULL = the context creates one) */
+    int fields;             /* M2_FIELDS_* */
 } m2_opts;
 
 typedef struct {
@@ -70,6 +79,7 @@ typedef struct {
     uint32_t rows, row_len, cols_per_cta, span;   /* large-path plan */
     uint64_t device_bytes;  /* device memory held by the context */
     uint32_t fused_cols;    /* 1: the inverse column pass and the next forward one run as one launch */
+    int fields;             /* M2_FIELDS_* */
 } m2_info_t;
 
 /* Replaces main()'s setup (mersenne2_gpu.cpp:3727-4028): exponent -> transform,
@@ -209,6 +219,8 @@ int m2_carry_normalize(uint32_t p, const int64_t* digits, const int64_t* seg_car
 
 /* Digit widths (n bytes) of exponent p, without a device; and log2 n. */
 int m2_layout(uint32_t p, int* ln, uint64_t* n, uint8_t* widths /* may be NULL */);
+/* The same for either field set (M2_FIELDS_*). */
+int m2_layout_fields(uint32_t p, int fields, int* ln, uint64_t* n, uint8_t* widths /* may be NULL */);
 
 const char* m2_strerror(int code);
 

@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(_PKG, "libm2gpu.so")
 
 MODE_LL, MODE_PRP, MODE_PRP3 = 0, 1, 2
 PATH_AUTO, PATH_SMALL, PATH_LARGE = 0, 1, 2
+FIELDS_DUAL, FIELDS_GF61 = 0, 1
 _MODES = {"ll": MODE_LL, "prp": MODE_PRP, "prp3": MODE_PRP3}
 
 # every symbol include/m2gpu.h declares
@@ -25,7 +26,7 @@ EXPORTS = (
     "m2_verdict", "m2_info", "m2_destroy", "m2_layout", "m2_strerror", "m2_batch_run",
     "m2_profile", "m2_launches_for", "m2_measure_mul_peak", "m2_square_noalloc",
     "m2_srv_create", "m2_srv_submit", "m2_srv_step", "m2_srv_poll", "m2_srv_stats_get", "m2_srv_destroy",
-    "m2_last_error", "m2_carry_normalize", "m2_batch_tuned",
+    "m2_last_error", "m2_carry_normalize", "m2_batch_tuned", "m2_layout_fields",
 )
 
 
@@ -38,14 +39,15 @@ class M2Error(RuntimeError):
 
 class _Opts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("wg", ctypes.c_uint32), ("carry_pairs", ctypes.c_uint32),
-                ("path", ctypes.c_int), ("stream", ctypes.c_void_p)]
+                ("path", ctypes.c_int), ("stream", ctypes.c_void_p), ("fields", ctypes.c_int)]
 
 
 class _Info(ctypes.Structure):
     _fields_ = [("p", ctypes.c_uint32), ("mode", ctypes.c_int), ("ln", ctypes.c_int), ("n", ctypes.c_uint64),
                 ("iteration", ctypes.c_uint32), ("total_iters", ctypes.c_uint32), ("path", ctypes.c_int),
                 ("rows", ctypes.c_uint32), ("row_len", ctypes.c_uint32), ("cols_per_cta", ctypes.c_uint32),
-                ("span", ctypes.c_uint32), ("device_bytes", ctypes.c_uint64), ("fused_cols", ctypes.c_uint32)]
+                ("span", ctypes.c_uint32), ("device_bytes", ctypes.c_uint64), ("fused_cols", ctypes.c_uint32),
+                ("fields", ctypes.c_int)]
 
 
 class _StageTime(ctypes.Structure):
@@ -79,6 +81,7 @@ def _lib() -> ctypes.CDLL:
         L.m2_destroy.argtypes = [vp]
         L.m2_destroy.restype = None
         L.m2_layout.argtypes = [u32, ctypes.POINTER(i), ctypes.POINTER(u64), vp]
+        L.m2_layout_fields.argtypes = [u32, i, ctypes.POINTER(i), ctypes.POINTER(u64), vp]
         L.m2_strerror.argtypes = [i]
         L.m2_strerror.restype = ctypes.c_char_p
         L.m2_batch_run.argtypes = [vp, vp, vp, ctypes.c_size_t, vp, vp, i, ctypes.POINTER(_BatchStats)]
@@ -103,13 +106,13 @@ def _check(rc: int, what: str) -> None:
         raise M2Error(rc, what)
 
 
-def layout(p: int) -> tuple[int, int, np.ndarray]:
-    """(log2 n, n, digit widths) of exponent p; no device needed."""
+def layout(p: int, fields: int = FIELDS_DUAL) -> tuple[int, int, np.ndarray]:
+    """(log2 n, n, digit widths) of exponent p for a field set; no device needed."""
     L = _lib()
     ln, n = ctypes.c_int(), ctypes.c_uint64()
-    _check(L.m2_layout(p, ctypes.byref(ln), ctypes.byref(n), None), "m2_layout")
+    _check(L.m2_layout_fields(p, fields, ctypes.byref(ln), ctypes.byref(n), None), "m2_layout_fields")
     w = np.zeros(n.value, dtype=np.uint8)
-    _check(L.m2_layout(p, ctypes.byref(ln), ctypes.byref(n), w.ctypes.data), "m2_layout")
+    _check(L.m2_layout_fields(p, fields, ctypes.byref(ln), ctypes.byref(n), w.ctypes.data), "m2_layout_fields")
     return ln.value, n.value, w
 
 
@@ -132,18 +135,19 @@ class Info:
     span: int
     device_bytes: int
     fused_cols: int
+    fields: int
 
 
 class Engine:
     """One test of 2^p - 1 on one GPU (wraps an m2_ctx)."""
 
     def __init__(self, p: int, mode: int | str = MODE_PRP, device: int = 0, path: int = PATH_AUTO,
-                 wg: int = 0, carry_pairs: int = 0, stream: int | None = None):
+                 wg: int = 0, carry_pairs: int = 0, stream: int | None = None, fields: int = FIELDS_DUAL):
         if isinstance(mode, str):
             mode = _MODES[mode.lower()]
         self._L = _lib()
         self._h = ctypes.c_void_p()
-        o = _Opts(device, wg, carry_pairs, path, stream)
+        o = _Opts(device, wg, carry_pairs, path, stream, fields)
         _check(self._L.m2_create(ctypes.byref(self._h), p, mode, ctypes.byref(o)), f"m2_create(p={p})")
         self.p, self.mode = p, mode
         self.info()
@@ -170,7 +174,7 @@ class Engine:
         _check(self._L.m2_info(self._h, ctypes.byref(i)), "m2_info")
         self.n = i.n
         return Info(i.p, i.mode, i.ln, i.n, i.iteration, i.total_iters, i.path, i.rows, i.row_len,
-                    i.cols_per_cta, i.span, i.device_bytes, i.fused_cols)
+                    i.cols_per_cta, i.span, i.device_bytes, i.fused_cols, i.fields)
 
     def iterate(self, k: int) -> None:
         _check(self._L.m2_iterate(self._h, k), "m2_iterate")

@@ -144,6 +144,7 @@ struct m2_ctx {
     uint2* d_zb = nullptr;
     unsigned* d_flags = nullptr;
     bool fused = false;        // inverse and next forward column pass as one cooperative launch
+    bool gf61 = false;         // GF(P61^2)-only transform (M2_FIELDS_GF61)
     // GRAPH_ITERS iterations of the three-pass path captured once and replayed
     cudaGraphExec_t graph = nullptr;
     bool graph_failed = false;
@@ -277,9 +278,12 @@ const char* m2_strerror(int code) {
     }
 }
 
-int m2_layout(uint32_t p, int* ln, uint64_t* n, uint8_t* widths) {
-    if (p < 3) return M2_EINVAL;
-    m2::Layout L = m2::make_layout(p);
+int m2_layout(uint32_t p, int* ln, uint64_t* n, uint8_t* widths) { return m2_layout_fields(p, M2_FIELDS_DUAL, ln, n, widths); }
+
+int m2_layout_fields(uint32_t p, int fields, int* ln, uint64_t* n, uint8_t* widths) {
+    if (p < 3 || (fields != M2_FIELDS_DUAL && fields != M2_FIELDS_GF61)) return M2_EINVAL;
+    if (m2::transform_log2(p, fields == M2_FIELDS_GF61 ? 61 : 92) > 30) return M2_EUNSUPPORTED;
+    m2::Layout L = m2::make_layout(p, fields == M2_FIELDS_GF61 ? 61 : 92);
     if (ln) *ln = L.ln;
     if (n) *n = L.n;
     if (widths) std::memcpy(widths, L.width.data(), L.n);
@@ -292,10 +296,13 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
     if (p < 3 || mode < M2_MODE_LL || mode > M2_MODE_PRP3) return M2_EINVAL;
     m2_opts o{};
     if (opts) o = *opts;
-    if (m2::transform_log2(p) > 30) return M2_EUNSUPPORTED;
+    if (o.fields != M2_FIELDS_DUAL && o.fields != M2_FIELDS_GF61) return M2_EINVAL;
+    const bool gf61 = (o.fields == M2_FIELDS_GF61);
+    if (m2::transform_log2(p, gf61 ? 61 : 92) > (gf61 ? 14 : 30)) return M2_EUNSUPPORTED;
     std::unique_ptr<m2_ctx> c(new (std::nothrow) m2_ctx());
     if (!c) return M2_ENOMEM;
-    c->L = m2::make_layout(p);
+    c->L = m2::make_layout(p, gf61 ? 61 : 92);
+    c->gf61 = gf61;
     c->mode = mode;
     c->device = o.device;
     if (cudaSetDevice(o.device) != cudaSuccess) { cudaGetLastError(); return M2_EINVAL; }
@@ -304,7 +311,8 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
     int path = o.path;
     // a lone test of h >= 2048 runs faster on the three-pass path's many CTAs
     // than in one CTA (the one-CTA path pays off when many tests share a launch)
-    if (path == M2_PATH_AUTO) path = (h <= 1024) ? M2_PATH_SMALL : M2_PATH_LARGE;
+    if (path == M2_PATH_AUTO) path = (h <= 1024 || gf61) ? M2_PATH_SMALL : M2_PATH_LARGE;
+    if (gf61 && path != M2_PATH_SMALL) return M2_EUNSUPPORTED;   // the one-CTA kernel only
     if (path == M2_PATH_SMALL && h > 8192) return M2_EUNSUPPORTED;
     if (path == M2_PATH_LARGE && !plan_large(c->L, c->span, o.carry_pairs, c->plan)) return M2_EUNSUPPORTED;
     c->path = path;
@@ -336,6 +344,7 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
         t.tw4 = raw->tw.tw4; t.tc = raw->tw.tc; t.status = raw->d_status;
         t.p = p; t.iters = 0; t.ln = raw->L.ln; t.mode = mode; t.span = raw->span;
         t.carry_threads = raw->carry_threads;
+        t.gf61_only = gf61 ? 1 : 0;
         raw->h_test = t;
         if (cudaMemcpyAsync(raw->d_test, &raw->h_test, sizeof(t), cudaMemcpyHostToDevice, raw->stream) != cudaSuccess) {
             m2_destroy(c.release());
@@ -509,6 +518,7 @@ int m2_info(m2_ctx* c, m2_info_t* info) {
     else { info->rows = 1; info->row_len = (uint32_t)c->L.h; info->cols_per_cta = (uint32_t)c->threads; }
     info->device_bytes = c->bytes;
     info->fused_cols = c->fused ? 1u : 0u;
+    info->fields = c->gf61 ? M2_FIELDS_GF61 : M2_FIELDS_DUAL;
     return M2_OK;
 }
 

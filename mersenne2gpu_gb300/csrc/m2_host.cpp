@@ -98,17 +98,17 @@ static inline u64 bitrev(u64 i, int bits) {
 }
 
 // ---------------- layout ----------------
-int transform_log2(u64 p) {
+int transform_log2(u64 p, int bound) {
     int ln = 2;
     u64 w;
-    do { ++ln; w = p >> ln; } while (u64(ln) + 2 * (w + 1) >= 92);
+    do { ++ln; w = p >> ln; } while (u64(ln) + 2 * (w + 1) >= u64(bound));
     return ln;
 }
 
-Layout make_layout(u32 p) {
+Layout make_layout(u32 p, int bound) {
     Layout L;
     L.p = p;
-    L.ln = transform_log2(p);
+    L.ln = transform_log2(p, bound);
     L.n = u64(1) << L.ln;
     L.h = L.n / 2;
     L.q = u32(p >> L.ln);

@@ -27,8 +27,10 @@ struct alignas(8) Dual {
 };
 static_assert(sizeof(Dual) == 24, "Dual must be 24 bytes");
 
-// Smallest ln >= 3 with ln + 2((p >> ln) + 1) < 92 (mersenne2_gpu.cpp:286-293).
-int transform_log2(u64 p);
+// Smallest ln >= 3 with ln + 2((p >> ln) + 1) < bound: 92 for the two fields
+// (mersenne2_gpu.cpp:286-293), 61 for GF(P61^2) alone
+// (gf61_ntt_prp_opencl_inplace_nobitrev_fused.cpp:124-132).
+int transform_log2(u64 p, int bound = 92);
 
 struct Layout {
     u32 p = 0;
@@ -40,7 +42,7 @@ struct Layout {
     std::vector<uint8_t> w31;     // n shifts mod 31
     std::vector<u64> bitpos;      // n+1 bit positions ceil(p j / n)
 };
-Layout make_layout(u32 p);
+Layout make_layout(u32 p, int bound = 92);
 
 // Roots of unity of this engine: g61 of order 2^62 in GF(P61^2) and g31 of
 // order 2^32 in GF(P31^2), chosen so that the order-4 root is +i.

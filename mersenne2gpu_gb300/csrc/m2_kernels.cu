@@ -76,12 +76,22 @@ __device__ __forceinline__ u32 unrot61(u32 s, int ln) { const u32 t = (s + (u32)
 __device__ __forceinline__ u32 unrot31(u32 s, int ln) { const u32 t = (s + (u32)ln + 1u) % 31u; return t ? 31u - t : 0u; }
 
 // unweight element k (digits 2k, 2k+1) and return the two signed convolution words
+// GF(P61)-only transforms: the residue in (-P61/2, P61/2] is the word itself
+__device__ __forceinline__ i128 signed61(u64 a) {
+    a = full61(a);
+    return (a > (P61 >> 1)) ? (i128)a - (i128)P61 : (i128)a;
+}
 __device__ __forceinline__ void unweigh_crt(const E& v, u64 j, const unsigned char* w61, const unsigned char* w31, int ln,
-                                            int mode, i128& z0, i128& z1) {
+                                            int mode, int gf61_only, i128& z0, i128& z1) {
     const u64 a = rotl61(fold61(v.a), unrot61(w61[j], ln)), b = rotl61(fold61(v.b), unrot61(w61[j + 1], ln));
-    const u32 c = rotl31(v.c, unrot31(w31[j], ln)), d = rotl31(v.d, unrot31(w31[j + 1], ln));
-    z0 = crt_signed(a, c);
-    z1 = crt_signed(b, d);
+    if (gf61_only) {
+        z0 = signed61(a);
+        z1 = signed61(b);
+    } else {
+        const u32 c = rotl31(v.c, unrot31(w31[j], ln)), d = rotl31(v.d, unrot31(w31[j + 1], ln));
+        z0 = crt_signed(a, c);
+        z1 = crt_signed(b, d);
+    }
     if (mode == PRP3) { z0 *= 3; z1 *= 3; }
 }
 
@@ -179,7 +189,7 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
                 i128 c = 0;
                 for (u32 k = 0; k < h; ++k) {
                     i128 z0, z1;
-                    unweigh_crt(z.ld(k), 2ull * k, T.w61, T.w31, ln, T.mode, z0, z1);
+                    unweigh_crt(z.ld(k), 2ull * k, T.w61, T.w31, ln, T.mode, T.gf61_only, z0, z1);
                     if (T.mode == LL && k == 0) z0 -= 2;
                     const i64 d0 = split_balanced(z0 + c, width_of(p, ln, 2ull * k), c);
                     const i64 d1 = split_balanced(z1 + c, width_of(p, ln, 2ull * k + 1), c);
@@ -204,7 +214,7 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
                 for (u32 u = 0; u < D; u += 2) {
                     const u32 k = (u32)((j0 + u) >> 1);
                     i128 z0, z1;
-                    unweigh_crt(z.ld(k), 2ull * k, T.w61, T.w31, ln, T.mode, z0, z1);
+                    unweigh_crt(z.ld(k), 2ull * k, T.w61, T.w31, ln, T.mode, T.gf61_only, z0, z1);
                     if (T.mode == LL && k == 0) z0 -= 2;
                     const i64 d0 = split_balanced(z0 + c, width_of(p, ln, 2ull * k), c);
                     const i64 d1 = split_balanced(z1 + c, width_of(p, ln, 2ull * k + 1), c);
@@ -502,7 +512,7 @@ __global__ void __launch_bounds__(LTC, 2) k_cols_inv(LargePlan P, LargeBufs bf) 
         for (int cc = 0; cc < C; ++cc) {
             const u64 e = e0 + cc, j = 2 * e;
             i128 z0, z1;
-            unweigh_crt(z.ld(t * C + cc), j, bf.w61, bf.w31, ln, P.mode, z0, z1);
+            unweigh_crt(z.ld(t * C + cc), j, bf.w61, bf.w31, ln, P.mode, 0, z0, z1);
             if (P.mode == LL && e == 0) z0 -= 2;
             const i64 d0 = split_balanced(z0 + c, width_of(p, ln, j), c);
             const i64 d1 = split_balanced(z1 + c, width_of(p, ln, j + 1), c);

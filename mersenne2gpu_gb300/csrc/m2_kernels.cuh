@@ -27,6 +27,7 @@ struct SmallTest {
     int mode;
     int span;                 // carry span (digits normalized after a segment carry)
     int carry_threads;        // threads taking part in the segmented carry (0 = one thread, full normalization)
+    int gf61_only;            // 1: the GF(P61) residue alone is the convolution word (no CRT)
 };
 
 // Plan of the three-pass path for one transform length.

@@ -10,7 +10,8 @@
 //             [-N max_iters] [--show-defaults] [--enable-chunk64] [--debug-plan]
 //             [--debug-stage-selftest] [--debug-cppint-every N] [--debug-cppint-max-iter N]
 //
-// Additions: the mode word prp3 (x <- 3 x^2, the GF61 prototype's PRP), --res64
+// Additions: the mode word prp3 (x <- 3 x^2, the GF61 prototype's PRP), --gf61
+// (GF(P61^2) alone with that prototype's size rule), --res64
 // (append the 64-bit residue to every progress line), --path small|large,
 // --checkpoint FILE / --resume FILE (state files: magic, p, mode, iteration, n,
 // canonical digits, FNV-1a checksum; written through a temporary file), and
@@ -117,6 +118,7 @@ int main(int argc, char* argv[]) {
     bool show_defaults_only = false, report_every_set = false, debug_plan = false, want_res64 = false;
     uint32_t debug_cppint_every = 0u, debug_cppint_max_iter = 0u;
     int path = M2_PATH_AUTO;
+    int fields = M2_FIELDS_DUAL;
     std::string checkpoint, resume;
 
     auto need = [&](int& i, const char* what) -> const char* {
@@ -155,6 +157,8 @@ int main(int argc, char* argv[]) {
             debug_cppint_max_iter = (uint32_t)std::strtoul(need(i, "value after --debug-cppint-max-iter"), nullptr, 10);
         } else if (arg == "--res64") {
             want_res64 = true;
+        } else if (arg == "--gf61") {
+            fields = M2_FIELDS_GF61;
         } else if (arg == "--path") {
             const std::string v = need(i, "small|large after --path");
             path = v == "small" ? M2_PATH_SMALL : (v == "large" ? M2_PATH_LARGE : M2_PATH_AUTO);
@@ -181,7 +185,7 @@ int main(int argc, char* argv[]) {
 
     int ln = 0;
     uint64_t n = 0;
-    int rc = m2_layout(p, &ln, &n, nullptr);
+    int rc = m2_layout_fields(p, fields, &ln, &n, nullptr);
     if (rc) return fail(rc, "m2_layout");
     const uint64_t h = n >> 1;
     std::cout << "p=" << p << ", ln=" << ln << ", transform=" << h << " (n=" << n << ")\n";
@@ -217,6 +221,7 @@ int main(int argc, char* argv[]) {
     o.wg = wg_override;
     o.carry_pairs = carry_pairs_override;
     o.path = path;
+    o.fields = fields;
     m2_ctx* ctx = nullptr;
     if ((rc = m2_create(&ctx, p, mode, &o))) return fail(rc, "m2_create");
     m2_info_t info{};

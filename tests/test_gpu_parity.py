@@ -108,3 +108,34 @@ def test_contexts_of_different_plans_coexist(m2, oracle_mod):
         o2 = oracle_mod.Oracle(756839, 1)
         o2.iterate(5)
         _cmp(small.digits(), o2.digits(), "later, smaller plan")
+
+
+@pytest.mark.parametrize("p", [5, 7, 13, 31, 61, 89, 107, 127, 521, 607, 1279])
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_gf61_only_full_runs_exact(m2, oracle_mod, p, mode):
+    """GF(P61^2)-only transforms (the GF61 prototype's size rule): full runs give
+    the exact residue and verdict."""
+    with m2.Engine(p, mode, fields=m2.FIELDS_GF61) as e:
+        assert e.info().fields == m2.FIELDS_GF61 and e.info().ln == m2.layout(p, m2.FIELDS_GF61)[0]
+        iters = m2.total_iterations(p, mode)
+        e.iterate(iters)
+        want = oracle_mod.python_chain(p, mode, iters) % ((1 << p) - 1)
+        assert e.res64() == want & ((1 << 64) - 1)
+        assert e.verdict() == (want == {0: 0, 1: 9 % ((1 << p) - 1), 2: 3 % ((1 << p) - 1)}[mode])
+
+
+@pytest.mark.parametrize("p", [9941, 44497, 132049, 216091, 376831])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_gf61_only_matches_dual_fields(m2, p, mode):
+    """Same residues as the dual-field engine, in a layout of as many or more digits."""
+    with m2.Engine(p, mode, fields=m2.FIELDS_GF61) as a, m2.Engine(p, mode) as b:
+        assert a.info().n >= b.info().n
+        for _ in range(3):
+            a.iterate(700)
+            b.iterate(700)
+            assert a.res64() == b.res64(), p
+
+
+def test_gf61_only_refuses_large_transforms(m2):
+    with pytest.raises(m2.M2Error, match=r"\(-6\)"):
+        m2.Engine(2976221, 1, fields=m2.FIELDS_GF61)

@@ -100,3 +100,28 @@ def test_cli_first_line_without_gpu(m2):
     r = subprocess.run([_cli(), "57885161", "prp"], capture_output=True, text=True)
     assert r.stdout.splitlines()[0] == "p=57885161, ln=21, transform=1048576 (n=2097152)"
     assert r.returncode == 1
+
+
+def _gf61_log2(p):
+    """The GF61 prototype's size rule (gf61_ntt_prp_opencl_inplace_nobitrev_fused.cpp:124-132)."""
+    ln = 2
+    while True:
+        ln += 1
+        if ln + 2 * ((p >> ln) + 1) < 61:
+            return ln
+
+
+@pytest.mark.parametrize("p", [3, 7, 31, 89, 127, 521, 9941, 44497, 132049, 216091, 376831])
+def test_gf61_layout_follows_the_prototype_rule(m2, p):
+    ln, n, w = m2.layout(p, m2.FIELDS_GF61)
+    assert ln == _gf61_log2(p) and n == 1 << ln
+    assert int(w.sum()) == p and set(np.unique(w)) <= {p >> ln, (p >> ln) + 1}
+
+
+def test_cli_gf61_first_line_without_gpu(m2):
+    from conftest import have_gpu
+    if have_gpu():
+        pytest.skip("a GPU is present; covered by the GPU tests")
+    r = subprocess.run([_cli(), "216091", "prp", "--gf61"], capture_output=True, text=True)
+    assert r.stdout.splitlines()[0] == "p=216091, ln=14, transform=8192 (n=16384)"
+    assert r.returncode == 1
