@@ -172,9 +172,9 @@ bool plan_large(const m2::Layout& L, int span, u32 carry_pairs, m2k::LargePlan& 
     P.ln = L.ln; P.L = Lh; P.L1 = L1; P.L2 = L2;
     P.R = 1u << L1; P.B = 1u << L2;
     P.span = span; P.p = L.p;
-    // columns per CTA: 4 (more CTAs for the small grids of mid-size transforms),
-    // 8 for the 256 x 2048 plan (n = 2^20), where it measured fastest
-    u32 C = (P.R == 256 && P.B == 2048) ? 8 : 4;
+    // columns per CTA: 4 (the quad-shuffle column kernels' shape for R = 256
+    // and 1024, and more CTAs for the small grids of the other mid-size plans)
+    u32 C = 4;
     if (carry_pairs >= 4 && carry_pairs <= 16 && (carry_pairs & (carry_pairs - 1)) == 0) C = carry_pairs;
     while (2 * C < (u32)span + 1 && C < 16) C <<= 1;
     if (2 * C < (u32)span + 1 || C > P.B) return false;

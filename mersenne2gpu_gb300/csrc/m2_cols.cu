@@ -1,8 +1,11 @@
-// m2_cols.cu -- column passes of the three-pass path for R = 1024 rows and
-// C = 4 columns per CTA (the plans of n = 2^21 and 2^22), with the radix-16
-// passes spread over lane quads as in the row pass.
+// m2_cols.cu -- column passes of the three-pass path for R = 1024 rows (n =
+// 2^21, 2^22) and R = 256 rows with rows of 1024 or 2048 (n = 2^19, 2^20), C =
+// 4 columns per CTA, with the radix-16 passes spread over lane quads as in the
+// row pass.  R = 256 has four levels (passes A and B) and copies between
+// shared and global memory where R = 1024 runs pass C.
 //
-// k_cols_fwd_q (one CTA per group of 4 columns, 512 threads):
+// k_cols_fwd_q (one CTA per group of 4 columns; 512 threads for R = 1024,
+// 128 for R = 256):
 //   row stage  each thread takes whole rows: applies the segment carry that
 //              the previous k_cols_inv_q left for the row's 8 digits (the carry
 //              of the segment before it), converts to both fields and weights;
@@ -25,7 +28,9 @@ namespace m2k {
 
 namespace {
 
-constexpr int CR = 1024, CC = 4, CNT = 512;
+constexpr int CC = 4;
+// threads of a CTA for R = CR rows: 8 elements each
+template <int CR> struct ColShape { static constexpr int CNT = CR * CC / 8; };
 
 __device__ __forceinline__ u32 swzc(u32 e) {
     u32 x = 0;
@@ -177,8 +182,9 @@ __device__ __forceinline__ void colpass_inv(const S6c& z, u32 base, u32 stride, 
 // row's segment), fields, weights.  Digits come from global memory, or from
 // the CTA's own shared slots (the fused kernel), where each element slot of a
 // row holds its two digits in the al/ah and bl/bh words.
-template <bool FROM_SMEM>
+template <int CR, bool FROM_SMEM>
 __device__ __forceinline__ void fwd_row_stage(const S6c& z, const LargePlan& P, const LargeBufs& bf, u32 g) {
+    constexpr int CNT = ColShape<CR>::CNT;
     const u32 B = P.B, G = P.G, tid = threadIdx.x;
     const u64 RG = (u64)CR * G;
     const u32 p = P.p;
@@ -218,65 +224,94 @@ __device__ __forceinline__ void fwd_row_stage(const S6c& z, const LargePlan& P, 
     }
 }
 
-// forward passes A, B (shared memory) and C (to global memory)
+// forward passes A (levels 1-2) and B (levels 3-4) in shared memory, then for
+// R = 1024 pass C (level 5, blocks of 4 rows) on the way to global memory, for
+// R = 256 (4 levels) a plain copy to global memory
+template <int CR>
 __device__ __forceinline__ void fwd_passes(const S6c& z, const LargePlan& P, const LargeBufs& bf, u32 g) {
+    constexpr int CNT = ColShape<CR>::CNT;
+    constexpr u32 MB = CR / 16, SB = (CR >= 256) ? CR / 256 : 1;   // pass B block rows and stride
     const u32 B = P.B, tid = threadIdx.x, l = tid & 3u;
-    // pass A: levels 1-2 (blocks of 1024 and 256 rows)
+    // pass A: levels 1-2 (blocks of CR and CR/4 rows)
 #pragma unroll 1
     for (u32 L = tid; L < (u32)(CC * CR / 4); L += CNT) {
         const u32 sc = L >> 2, c = sc % CC, i = sc / CC;
         colpass_fwd(z, i * CC + c, (CR / 16) * CC, l, bf.tw4, 1, 0, 0);
     }
     __syncthreads();
-    // pass B: levels 3-4 (blocks of 64 and 16 rows)
+    // pass B: levels 3-4 (blocks of CR/16 and CR/64 rows)
 #pragma unroll 1
     for (u32 L = tid; L < (u32)(CC * CR / 4); L += CNT) {
-        const u32 sc = L >> 2, c = sc % CC, rest = sc / CC, jb = rest / 4, ib = rest % 4;
-        colpass_fwd(z, (jb * 64 + ib) * CC + c, 4 * CC, l, bf.tw4, 16, jb, 4 * jb);
+        const u32 sc = L >> 2, c = sc % CC, rest = sc / CC, jb = rest / SB, ib = rest % SB;
+        colpass_fwd(z, (jb * MB + ib) * CC + c, SB * CC, l, bf.tw4, 16, jb, 4 * jb);
     }
     __syncthreads();
-    // pass C: level 5 (blocks of 4 rows), to global memory
+    if (CR == 1024) {
+        // pass C: level 5 (blocks of 4 rows), to global memory
 #pragma unroll 1
-    for (u32 Gq = tid; Gq < (u32)(CC * CR / 4); Gq += CNT) {
-        const u32 c = Gq % CC, J = Gq / CC;
-        E x[4];
+        for (u32 Gq = tid; Gq < (u32)(CC * CR / 4); Gq += CNT) {
+            const u32 c = Gq % CC, J = Gq / CC;
+            E x[4];
 #pragma unroll
-        for (int b = 0; b < 4; ++b) x[b] = z.ld((4 * J + b) * CC + c);
-        const Tri t = tri(bf.tw4, 256, J);
-        dif4(x[0], x[1], x[2], x[3], t.r1, t.r2, t.r3);
+            for (int b = 0; b < 4; ++b) x[b] = z.ld((4 * J + b) * CC + c);
+            const Tri t = tri(bf.tw4, 256, J);
+            dif4(x[0], x[1], x[2], x[3], t.r1, t.r2, t.r3);
 #pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            const u64 e = (u64)(4 * J + b) * B + (u64)g * CC + c;
-            bf.za[e] = make_ulonglong2(x[b].a, x[b].b);
-            bf.zb[e] = make_uint2(x[b].c, x[b].d);
+            for (int b = 0; b < 4; ++b) {
+                const u64 e = (u64)(4 * J + b) * B + (u64)g * CC + c;
+                bf.za[e] = make_ulonglong2(x[b].a, x[b].b);
+                bf.zb[e] = make_uint2(x[b].c, x[b].d);
+            }
+        }
+    } else {
+#pragma unroll 1
+        for (u32 e = tid; e < (u32)(CC * CR); e += CNT) {
+            const E v = z.ld(e);
+            const u64 o = (u64)(e / CC) * B + (u64)g * CC + e % CC;
+            bf.za[o] = make_ulonglong2(v.a, v.b);
+            bf.zb[o] = make_uint2(v.c, v.d);
         }
     }
 }
 
-// inverse passes C (from global memory), B and A
+// inverse passes: for R = 1024 pass C (level 5) from global memory, for R =
+// 256 a plain copy from global memory; then B and A
+template <int CR>
 __device__ __forceinline__ void inv_passes(const S6c& z, const LargePlan& P, const LargeBufs& bf, u32 g) {
+    constexpr int CNT = ColShape<CR>::CNT;
+    constexpr u32 MB = CR / 16, SB = (CR >= 256) ? CR / 256 : 1;
     const u32 B = P.B, tid = threadIdx.x, l = tid & 3u;
+    if (CR == 1024) {
 #pragma unroll 1
-    for (u32 Gq = tid; Gq < (u32)(CC * CR / 4); Gq += CNT) {
-        const u32 c = Gq % CC, J = Gq / CC;
-        E x[4];
+        for (u32 Gq = tid; Gq < (u32)(CC * CR / 4); Gq += CNT) {
+            const u32 c = Gq % CC, J = Gq / CC;
+            E x[4];
 #pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            const u64 e = (u64)(4 * J + b) * B + (u64)g * CC + c;
-            const ulonglong2 va = bf.za[e];
-            const uint2 vb = bf.zb[e];
-            x[b] = E{va.x, va.y, vb.x, vb.y};
+            for (int b = 0; b < 4; ++b) {
+                const u64 e = (u64)(4 * J + b) * B + (u64)g * CC + c;
+                const ulonglong2 va = bf.za[e];
+                const uint2 vb = bf.zb[e];
+                x[b] = E{va.x, va.y, vb.x, vb.y};
+            }
+            const Tri t = tri(bf.tw4, 256, J);
+            dit4(x[0], x[1], x[2], x[3], t.r1, t.r2, t.r3);
+#pragma unroll
+            for (int b = 0; b < 4; ++b) z.st((4 * J + b) * CC + c, x[b]);
         }
-        const Tri t = tri(bf.tw4, 256, J);
-        dit4(x[0], x[1], x[2], x[3], t.r1, t.r2, t.r3);
-#pragma unroll
-        for (int b = 0; b < 4; ++b) z.st((4 * J + b) * CC + c, x[b]);
+    } else {
+#pragma unroll 1
+        for (u32 e = tid; e < (u32)(CC * CR); e += CNT) {
+            const u64 o = (u64)(e / CC) * B + (u64)g * CC + e % CC;
+            const ulonglong2 va = bf.za[o];
+            const uint2 vb = bf.zb[o];
+            z.st(e, E{va.x, va.y, vb.x, vb.y});
+        }
     }
     __syncthreads();
 #pragma unroll 1
     for (u32 L = tid; L < (u32)(CC * CR / 4); L += CNT) {
-        const u32 sc = L >> 2, c = sc % CC, rest = sc / CC, jb = rest / 4, ib = rest % 4;
-        colpass_inv(z, (jb * 64 + ib) * CC + c, 4 * CC, l, bf.tw4, 16, jb, 4 * jb);
+        const u32 sc = L >> 2, c = sc % CC, rest = sc / CC, jb = rest / SB, ib = rest % SB;
+        colpass_inv(z, (jb * MB + ib) * CC + c, SB * CC, l, bf.tw4, 16, jb, 4 * jb);
     }
     __syncthreads();
 #pragma unroll 1
@@ -289,8 +324,9 @@ __device__ __forceinline__ void inv_passes(const S6c& z, const LargePlan& P, con
 // inverse row stage: unweight, CRT, carry within the row segment of 8 digits;
 // the digits go to global memory or back into the row's own shared slots, the
 // segment's carry out to global memory
-template <bool TO_SMEM>
+template <int CR, bool TO_SMEM>
 __device__ __forceinline__ void inv_row_stage(const S6c& z, const LargePlan& P, const LargeBufs& bf, u32 g) {
+    constexpr int CNT = ColShape<CR>::CNT;
     const u32 B = P.B, G = P.G, tid = threadIdx.x;
     const u32 p = P.p;
     const int ln = P.ln;
@@ -351,20 +387,24 @@ __device__ __forceinline__ void st_release(unsigned* a, unsigned v) {
 
 }  // namespace
 
-__global__ void __launch_bounds__(CNT, 2) k_cols_fwd_q(LargePlan P, LargeBufs bf) {
+// register budget 64 at every shape: two 512-thread CTAs (R = 1024) or eight
+// 128-thread CTAs (R = 256) per SM
+template <int CR>
+__global__ void __launch_bounds__(ColShape<CR>::CNT, 65536 / (64 * ColShape<CR>::CNT)) k_cols_fwd_q(LargePlan P, LargeBufs bf) {
     extern __shared__ __align__(16) unsigned char smem[];
     const S6c z = make_s6c(smem, CR * CC);
-    fwd_row_stage<false>(z, P, bf, blockIdx.x);
+    fwd_row_stage<CR, false>(z, P, bf, blockIdx.x);
     __syncthreads();
-    fwd_passes(z, P, bf, blockIdx.x);
+    fwd_passes<CR>(z, P, bf, blockIdx.x);
 }
 
-__global__ void __launch_bounds__(CNT, 2) k_cols_inv_q(LargePlan P, LargeBufs bf) {
+template <int CR>
+__global__ void __launch_bounds__(ColShape<CR>::CNT, 65536 / (64 * ColShape<CR>::CNT)) k_cols_inv_q(LargePlan P, LargeBufs bf) {
     extern __shared__ __align__(16) unsigned char smem[];
     const S6c z = make_s6c(smem, CR * CC);
-    inv_passes(z, P, bf, blockIdx.x);
+    inv_passes<CR>(z, P, bf, blockIdx.x);
     __syncthreads();
-    inv_row_stage<false>(z, P, bf, blockIdx.x);
+    inv_row_stage<CR, false>(z, P, bf, blockIdx.x);
 }
 
 // The inverse column pass of one squaring fused with the forward column pass
@@ -375,15 +415,16 @@ __global__ void __launch_bounds__(CNT, 2) k_cols_inv_q(LargePlan P, LargeBufs bf
 // once, so all flags are equal between launches) and waits, bounded, for its
 // predecessor's flag.  Launched cooperatively, so all G CTAs are resident and
 // the waits end; a wait that runs out sets ST_WAIT_TIMEOUT and the CTA goes on.
-__global__ void __launch_bounds__(CNT, 2) k_cols_mid_q(LargePlan P, LargeBufs bf) {
+template <int CR>
+__global__ void __launch_bounds__(ColShape<CR>::CNT, 65536 / (64 * ColShape<CR>::CNT)) k_cols_mid_q(LargePlan P, LargeBufs bf) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned s_epoch;
     const S6c z = make_s6c(smem, CR * CC);
     const u32 g = blockIdx.x, G = P.G;
     if (threadIdx.x == 0) s_epoch = bf.flags[g] + 1u;
-    inv_passes(z, P, bf, g);
+    inv_passes<CR>(z, P, bf, g);
     __syncthreads();
-    inv_row_stage<true>(z, P, bf, g);
+    inv_row_stage<CR, true>(z, P, bf, g);
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -397,49 +438,46 @@ __global__ void __launch_bounds__(CNT, 2) k_cols_mid_q(LargePlan P, LargeBufs bf
         }
     }
     __syncthreads();
-    fwd_row_stage<true>(z, P, bf, g);
+    fwd_row_stage<CR, true>(z, P, bf, g);
     __syncthreads();
-    fwd_passes(z, P, bf, g);
+    fwd_passes<CR>(z, P, bf, g);
 }
 
-bool cols_q_supported(const LargePlan& P) { return P.R == (u32)CR && P.C == (u32)CC && P.span < 2 * CC; }
+// R = 256 only with rows of 1024 or more: below that (G <= 128 CTAs of 128
+// threads) the generic kernels' larger CTAs measured faster
+bool cols_q_supported(const LargePlan& P) {
+    return (P.R == 1024u || (P.R == 256u && P.B >= 1024u)) && P.C == (u32)CC && P.span < 2 * CC;
+}
 
-cudaError_t cols_q_setup(const LargePlan& P) {
+namespace {
+template <int CR>
+cudaError_t setup_shape() {
     const int sm = (int)(24ull * CR * CC);
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(k_cols_fwd_q, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
-    if ((e = cudaFuncSetAttribute(k_cols_inv_q, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
-    if ((e = cudaFuncSetAttribute(k_cols_mid_q, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
-    if ((e = cudaFuncSetAttribute(k_cols_fwd_q, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
-    if ((e = cudaFuncSetAttribute(k_cols_inv_q, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
-    return cudaFuncSetAttribute(k_cols_mid_q, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if ((e = cudaFuncSetAttribute(k_cols_fwd_q<CR>, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
+    if ((e = cudaFuncSetAttribute(k_cols_inv_q<CR>, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
+    if ((e = cudaFuncSetAttribute(k_cols_mid_q<CR>, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
+    if ((e = cudaFuncSetAttribute(k_cols_fwd_q<CR>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
+    if ((e = cudaFuncSetAttribute(k_cols_inv_q<CR>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
+    return cudaFuncSetAttribute(k_cols_mid_q<CR>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
 }
-
-// true when all G CTAs of the fused kernel fit on the device at once
-bool cols_mid_supported(const LargePlan& P) {
-    if (!cols_q_supported(P)) return false;
+template <int CR>
+bool mid_fits(const LargePlan& P) {
     int dev = 0, sms = 0, per = 0, coop = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return false;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return false;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cols_mid_q, CNT, 24ull * CR * CC) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cols_mid_q<CR>, ColShape<CR>::CNT, 24ull * CR * CC) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
     return (long long)per * sms >= (long long)P.G;
 }
-
-cudaError_t launch_cols_q(const LargePlan& P, const LargeBufs& b, bool inverse, cudaStream_t s) {
-    const size_t sm = 24ull * CR * CC;
-    if (inverse) k_cols_inv_q<<<P.G, CNT, sm, s>>>(P, b);
-    else k_cols_fwd_q<<<P.G, CNT, sm, s>>>(P, b);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_cols_mid(const LargePlan& P, const LargeBufs& b, cudaStream_t s) {
+template <int CR>
+cudaError_t launch_mid(const LargePlan& P, const LargeBufs& b, cudaStream_t s) {
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(P.G);
-    cfg.blockDim = dim3(CNT);
+    cfg.blockDim = dim3(ColShape<CR>::CNT);
     cfg.dynamicSmemBytes = 24ull * CR * CC;
     cfg.stream = s;
     cudaLaunchAttribute at[1];
@@ -447,7 +485,33 @@ cudaError_t launch_cols_mid(const LargePlan& P, const LargeBufs& b, cudaStream_t
     at[0].val.cooperative = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_cols_mid_q, P, b);
+    return cudaLaunchKernelEx(&cfg, k_cols_mid_q<CR>, P, b);
+}
+}  // namespace
+
+cudaError_t cols_q_setup(const LargePlan& P) { return P.R == 1024u ? setup_shape<1024>() : setup_shape<256>(); }
+
+// true when all G CTAs of the fused kernel fit on the device at once
+bool cols_mid_supported(const LargePlan& P) {
+    if (!cols_q_supported(P)) return false;
+    return P.R == 1024u ? mid_fits<1024>(P) : mid_fits<256>(P);
+}
+
+cudaError_t launch_cols_q(const LargePlan& P, const LargeBufs& b, bool inverse, cudaStream_t s) {
+    if (P.R == 1024u) {
+        constexpr int CR = 1024;
+        if (inverse) k_cols_inv_q<CR><<<P.G, ColShape<CR>::CNT, 24ull * CR * CC, s>>>(P, b);
+        else k_cols_fwd_q<CR><<<P.G, ColShape<CR>::CNT, 24ull * CR * CC, s>>>(P, b);
+    } else {
+        constexpr int CR = 256;
+        if (inverse) k_cols_inv_q<CR><<<P.G, ColShape<CR>::CNT, 24ull * CR * CC, s>>>(P, b);
+        else k_cols_fwd_q<CR><<<P.G, ColShape<CR>::CNT, 24ull * CR * CC, s>>>(P, b);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cols_mid(const LargePlan& P, const LargeBufs& b, cudaStream_t s) {
+    return P.R == 1024u ? launch_mid<1024>(P, b, s) : launch_mid<256>(P, b, s);
 }
 
 }  // namespace m2k

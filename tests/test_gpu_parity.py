@@ -86,6 +86,22 @@ def test_large_path_long_rows_vs_oracle(m2, oracle_mod, p, mode):
     _cmp(got, o.digits(), f"large p={p} mode={mode}")
 
 
+@pytest.mark.parametrize("p", [2976221, 9437179, 18874367, 36700159])   # R = 256 rows: B = 256, 512, 1024, 2048
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_large_path_256_rows_vs_oracle(m2, oracle_mod, p, mode):
+    """R = 256 rows: the generic column kernels (B = 256, 512) and the quad-shuffle
+    ones with the fused column pass (B = 1024, 2048)."""
+    iters = 3
+    with m2.Engine(p, mode, path=m2.PATH_LARGE) as e:
+        info = e.info()
+        assert info.rows == 256 and info.cols_per_cta == 4
+        e.iterate(iters)
+        got = e.digits()
+    o = oracle_mod.Oracle(p, mode)
+    o.iterate(iters)
+    _cmp(got, o.digits(), f"large p={p} mode={mode}")
+
+
 @pytest.mark.parametrize("p", [9941, 44497, 132049])
 def test_paths_agree(m2, p):
     """The one-CTA path and the three-pass path give the same state."""
