@@ -217,6 +217,14 @@ int m2_square_noalloc(uint32_t p, int mode, int64_t* digits, uint32_t iters, voi
 int m2_carry_normalize(uint32_t p, const int64_t* digits, const int64_t* seg_carries, uint32_t seg_digits,
                        uint64_t* out, void* stream);
 
+/* Test hook of the fused column kernel's bounded wait (no GPU fault): raises
+ * the epoch flag of column CTA 0 by 2^20, so in the next fused launch CTA 0
+ * waits for a flag value that its predecessor never writes; the wait gives up
+ * after its limit, the launch completes, and m2_sync reports M2_ETIMEOUT.  The
+ * state is then meaningless until m2_set_digits reloads it (which also resets
+ * the flags).  M2_EUNSUPPORTED when the context has no fused column pass. */
+int m2_test_stall_fused(m2_ctx* ctx);
+
 /* Digit widths (n bytes) of exponent p, without a device; and log2 n. */
 int m2_layout(uint32_t p, int* ln, uint64_t* n, uint8_t* widths /* may be NULL */);
 /* The same for either field set (M2_FIELDS_*). */

@@ -26,7 +26,7 @@ EXPORTS = (
     "m2_verdict", "m2_info", "m2_destroy", "m2_layout", "m2_strerror", "m2_batch_run",
     "m2_profile", "m2_launches_for", "m2_measure_mul_peak", "m2_square_noalloc",
     "m2_srv_create", "m2_srv_submit", "m2_srv_step", "m2_srv_poll", "m2_srv_stats_get", "m2_srv_destroy",
-    "m2_last_error", "m2_carry_normalize", "m2_batch_tuned", "m2_layout_fields",
+    "m2_last_error", "m2_carry_normalize", "m2_batch_tuned", "m2_layout_fields", "m2_test_stall_fused",
 )
 
 
@@ -91,6 +91,7 @@ def _lib() -> ctypes.CDLL:
         L.m2_measure_mul_peak.argtypes = [i, ctypes.POINTER(ctypes.c_double)]
         L.m2_square_noalloc.argtypes = [u32, i, vp, u32, vp]
         L.m2_carry_normalize.argtypes = [u32, vp, vp, u32, vp, vp]
+        L.m2_test_stall_fused.argtypes = [vp]
         L.m2_batch_tuned.argtypes = [i, i, ctypes.POINTER(i), ctypes.POINTER(ctypes.c_double)]
         L.m2_last_error.argtypes = []
         L.m2_last_error.restype = ctypes.c_char_p

@@ -506,6 +506,19 @@ int m2_carry_normalize(uint32_t p, const int64_t* digits, const int64_t* seg_car
     return st ? M2_ESTATE : M2_OK;
 }
 
+int m2_test_stall_fused(m2_ctx* c) {
+    if (!c) return M2_EINVAL;
+    if (!c->fused || !c->d_flags) return M2_EUNSUPPORTED;
+    if (cudaSetDevice(c->device) != cudaSuccess) return M2_ECUDA;
+    unsigned f0 = 0;
+    cudaError_t e = cudaMemcpyAsync(&f0, c->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    f0 += 1u << 20;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_flags, &f0, sizeof(unsigned), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? M2_OK : fail_cuda("m2_test_stall_fused", e);
+}
+
 int m2_info(m2_ctx* c, m2_info_t* info) {
     if (!c || !info) return M2_EINVAL;
     std::memset(info, 0, sizeof(*info));

@@ -155,3 +155,24 @@ def test_gf61_only_matches_dual_fields(m2, p, mode):
 def test_gf61_only_refuses_large_transforms(m2):
     with pytest.raises(m2.M2Error, match=r"\(-6\)"):
         m2.Engine(2976221, 1, fields=m2.FIELDS_GF61)
+
+
+def test_fused_wait_runs_out_and_reports_timeout(m2, oracle_mod):
+    """Failure detection without a GPU fault: the fused column kernel's flag
+    wait is made to run out (CTA 0's epoch raised past anything its
+    predecessor writes); the launch completes, m2_sync reports M2_ETIMEOUT, and
+    after a reload the context computes correct results again."""
+    p = 18874367
+    with m2.Engine(p, 1, path=m2.PATH_LARGE) as e:
+        assert e.info().fused_cols == 1
+        start = e.digits()
+        assert e._L.m2_test_stall_fused(e._h) == 0
+        e.iterate(3)                                 # fwd, rows, mid (CTA 0 waits out), rows, mid, rows, inv
+        with pytest.raises(m2.M2Error, match=r"\(-4\)"):
+            e.sync()
+        e.set_digits(start, 0)                       # reload: flags and status reset
+        e.iterate(3)
+        got = e.digits()
+    o = oracle_mod.Oracle(p, 1)
+    o.iterate(3)
+    _cmp(got, o.digits(), "after the timeout")
