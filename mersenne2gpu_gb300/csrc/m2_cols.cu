@@ -44,16 +44,20 @@ __device__ __forceinline__ u32 swzc(u32 e) {
     return e ^ x;
 }
 
+// The swizzle is linear over GF(2), so for an index a + b with a and b on
+// disjoint bits swzc(a + b) = swzc(a) ^ swzc(b): the passes swizzle a thread's
+// base once and reach each element with one XOR by a compile-time constant
+// (ldp/stp take swizzled indices).
 struct S6c {
     u32 *al, *ah, *bl, *bh, *c, *d;
-    __device__ __forceinline__ E ld(u32 e) const {
-        const u32 p = swzc(e);
+    __device__ __forceinline__ E ldp(u32 p) const {
         return E{(u64)al[p] | ((u64)ah[p] << 32), (u64)bl[p] | ((u64)bh[p] << 32), c[p], d[p]};
     }
-    __device__ __forceinline__ void st(u32 e, const E& v) const {
-        const u32 p = swzc(e);
+    __device__ __forceinline__ void stp(u32 p, const E& v) const {
         al[p] = (u32)v.a; ah[p] = (u32)(v.a >> 32); bl[p] = (u32)v.b; bh[p] = (u32)(v.b >> 32); c[p] = v.c; d[p] = v.d;
     }
+    __device__ __forceinline__ E ld(u32 e) const { return ldp(swzc(e)); }
+    __device__ __forceinline__ void st(u32 e, const E& v) const { stp(swzc(e), v); }
 };
 __device__ __forceinline__ S6c make_s6c(unsigned char* base, u32 ne) {
     u32* w = reinterpret_cast<u32*>(base);
@@ -150,28 +154,31 @@ __device__ __forceinline__ i64 crt_digit(u64 r61, u32 r31, u32 w, u32 mul, i64 s
     return (i64)(lo & ((1ull << w) - 1)) - ((i64)1 << (w - 1));
 }
 
-// the 16-element sub-column passes over the columns (rows i + stride k of a block)
+// the 16-element sub-column passes over the columns (rows i + stride k of a
+// block; base < stride, so base and stride k sit on disjoint bits)
 __device__ __forceinline__ void colpass_fwd(const S6c& z, u32 base, u32 stride, u32 l, const DTw* tw4, u64 SA_, u64 JA, u64 JB0) {
+    const u32 pb = swzc(base), pl = pb ^ swzc(stride * l), p4l = pb ^ swzc(stride * 4 * l);
     E x[4];
 #pragma unroll
-    for (int m = 0; m < 4; ++m) x[m] = z.ld(base + stride * (l + 4 * m));
+    for (int m = 0; m < 4; ++m) x[m] = z.ldp(pl ^ swzc(stride * 4 * m));
     if (SA_ == 1) dif4_1(x[0], x[1], x[2], x[3]);   // the first level: root 1
     else { const Tri A = tri(tw4, SA_, JA); dif4(x[0], x[1], x[2], x[3], A.r1, A.r2, A.r3); }
     quad_transpose(x, l);
     { const Tri Bt = tri(tw4, 4 * SA_, JB0 + l); dif4(x[0], x[1], x[2], x[3], Bt.r1, Bt.r2, Bt.r3); }
 #pragma unroll
-    for (int m = 0; m < 4; ++m) z.st(base + stride * (4 * l + m), x[m]);
+    for (int m = 0; m < 4; ++m) z.stp(p4l ^ swzc(stride * m), x[m]);
 }
 __device__ __forceinline__ void colpass_inv(const S6c& z, u32 base, u32 stride, u32 l, const DTw* tw4, u64 SA_, u64 JA, u64 JB0) {
+    const u32 pb = swzc(base), pl = pb ^ swzc(stride * l), p4l = pb ^ swzc(stride * 4 * l);
     E x[4];
 #pragma unroll
-    for (int m = 0; m < 4; ++m) x[m] = z.ld(base + stride * (4 * l + m));
+    for (int m = 0; m < 4; ++m) x[m] = z.ldp(p4l ^ swzc(stride * m));
     { const Tri Bt = tri(tw4, 4 * SA_, JB0 + l); dit4(x[0], x[1], x[2], x[3], Bt.r1, Bt.r2, Bt.r3); }
     quad_transpose(x, l);
     if (SA_ == 1) dit4_1(x[0], x[1], x[2], x[3]);   // the first level: root 1
     else { const Tri A = tri(tw4, SA_, JA); dit4(x[0], x[1], x[2], x[3], A.r1, A.r2, A.r3); }
 #pragma unroll
-    for (int m = 0; m < 4; ++m) z.st(base + stride * (l + 4 * m), x[m]);
+    for (int m = 0; m < 4; ++m) z.stp(pl ^ swzc(stride * 4 * m), x[m]);
 }
 
 // element (row r, column c) of the CTA's column group lives at r*CC + c
@@ -199,7 +206,7 @@ __device__ __forceinline__ void fwd_row_stage(const S6c& z, const LargePlan& P, 
         if (FROM_SMEM) {
 #pragma unroll
             for (int u = 0; u < CC; ++u) {
-                const u32 q = swzc(r * CC + u);
+                const u32 q = swzc(r * CC) ^ (u32)u;
                 d[2 * u] = (i64)((u64)z.al[q] | ((u64)z.ah[q] << 32));
                 d[2 * u + 1] = (i64)((u64)z.bl[q] | ((u64)z.bh[q] << 32));
             }
@@ -218,8 +225,9 @@ __device__ __forceinline__ void fwd_row_stage(const S6c& z, const LargePlan& P, 
 #pragma unroll
         for (int h2 = 0; h2 < 2; ++h2) {
             const uchar4 a = w61[h2], b = w31[h2];
-            z.st(r * CC + 2 * h2, weigh(d[4 * h2], d[4 * h2 + 1], a.x, a.y, b.x, b.y));
-            z.st(r * CC + 2 * h2 + 1, weigh(d[4 * h2 + 2], d[4 * h2 + 3], a.z, a.w, b.z, b.w));
+            const u32 pr = swzc(r * CC);
+            z.stp(pr ^ (u32)(2 * h2), weigh(d[4 * h2], d[4 * h2 + 1], a.x, a.y, b.x, b.y));
+            z.stp(pr ^ (u32)(2 * h2 + 1), weigh(d[4 * h2 + 2], d[4 * h2 + 3], a.z, a.w, b.z, b.w));
         }
     }
 }
@@ -251,9 +259,10 @@ __device__ __forceinline__ void fwd_passes(const S6c& z, const LargePlan& P, con
 #pragma unroll 1
         for (u32 Gq = tid; Gq < (u32)(CC * CR / 4); Gq += CNT) {
             const u32 c = Gq % CC, J = Gq / CC;
+            const u32 pj = swzc(4 * J * CC + c);     // swzc((4J + b) CC + c) = pj ^ b CC
             E x[4];
 #pragma unroll
-            for (int b = 0; b < 4; ++b) x[b] = z.ld((4 * J + b) * CC + c);
+            for (int b = 0; b < 4; ++b) x[b] = z.ldp(pj ^ (u32)(b * CC));
             const Tri t = tri(bf.tw4, 256, J);
             dif4(x[0], x[1], x[2], x[3], t.r1, t.r2, t.r3);
 #pragma unroll
@@ -295,8 +304,9 @@ __device__ __forceinline__ void inv_passes(const S6c& z, const LargePlan& P, con
             }
             const Tri t = tri(bf.tw4, 256, J);
             dit4(x[0], x[1], x[2], x[3], t.r1, t.r2, t.r3);
+            const u32 pj = swzc(4 * J * CC + c);
 #pragma unroll
-            for (int b = 0; b < 4; ++b) z.st((4 * J + b) * CC + c, x[b]);
+            for (int b = 0; b < 4; ++b) z.stp(pj ^ (u32)(b * CC), x[b]);
         }
     } else {
 #pragma unroll 1
@@ -348,7 +358,7 @@ __device__ __forceinline__ void inv_row_stage(const S6c& z, const LargePlan& P, 
 #pragma unroll
             for (int u = 0; u < 2; ++u) {
                 const u32 cc = 2 * h2 + u;
-                const E v = z.ld(r * CC + cc);
+                const E v = z.ldp(swzc(r * CC) ^ cc);
                 const u64 x0 = rotl61(fold61(v.a), unrot61f(s61[2 * u], ln1)), x1 = rotl61(fold61(v.b), unrot61f(s61[2 * u + 1], ln1));
                 const u32 y0 = rotl31(v.c, unrot31f(s31[2 * u], ln1)), y1 = rotl31(v.d, unrot31f(s31[2 * u + 1], ln1));
                 const u64 j = j0 + 2 * cc;
@@ -362,7 +372,7 @@ __device__ __forceinline__ void inv_row_stage(const S6c& z, const LargePlan& P, 
         if (TO_SMEM) {
 #pragma unroll
             for (int u = 0; u < CC; ++u) {
-                const u32 q = swzc(r * CC + u);
+                const u32 q = swzc(r * CC) ^ (u32)u;
                 z.al[q] = (u32)(u64)d[2 * u]; z.ah[q] = (u32)((u64)d[2 * u] >> 32);
                 z.bl[q] = (u32)(u64)d[2 * u + 1]; z.bh[q] = (u32)((u64)d[2 * u + 1] >> 32);
             }

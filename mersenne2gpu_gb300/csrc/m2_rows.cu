@@ -49,16 +49,21 @@ __device__ __forceinline__ u32 swz(u32 e) {
     return e ^ x;
 }
 
+// The swizzle is linear over GF(2) (it XORs masks selected by bits 5-11 into
+// bits 0-4), so for an index a + b with a and b on disjoint bits swz(a + b) =
+// swz(a) ^ swz(b): the passes swizzle a thread's base once and reach each
+// element with one XOR by a compile-time constant (ldp/stp take swizzled
+// indices).
 struct S6 {
     u32 *al, *ah, *bl, *bh, *c, *d;
-    __device__ __forceinline__ E ld(u32 e) const {
-        const u32 p = swz(e);
+    __device__ __forceinline__ E ldp(u32 p) const {
         return E{(u64)al[p] | ((u64)ah[p] << 32), (u64)bl[p] | ((u64)bh[p] << 32), c[p], d[p]};
     }
-    __device__ __forceinline__ void st(u32 e, const E& v) const {
-        const u32 p = swz(e);
+    __device__ __forceinline__ void stp(u32 p, const E& v) const {
         al[p] = (u32)v.a; ah[p] = (u32)(v.a >> 32); bl[p] = (u32)v.b; bh[p] = (u32)(v.b >> 32); c[p] = v.c; d[p] = v.d;
     }
+    __device__ __forceinline__ E ld(u32 e) const { return ldp(swz(e)); }
+    __device__ __forceinline__ void st(u32 e, const E& v) const { stp(swz(e), v); }
 };
 __device__ __forceinline__ S6 make_s6(unsigned char* base, u32 ne) {
     u32* w = reinterpret_cast<u32*>(base);
@@ -123,15 +128,16 @@ __device__ __forceinline__ void quad_transpose(E (&x)[4], u32 l) {
 }
 
 // A radix-16 pass on one sub-column of 16 elements e(k) = base + stride k,
-// spread over a quad: lane l loads k = l + 4m, runs the first radix-4 level
-// (block JA at SA_ blocks), transposes, runs the second level (block JB0 + l,
-// or JB0 + 3 - l when mirrored, at 4 SA_ blocks) and leaves k = 4l + m.
-// The inverse runs the same steps backwards.
+// spread over a quad: lane l loads k = l + 4m (load(m)), runs the first
+// radix-4 level (block JA at SA_ blocks), transposes, runs the second level
+// (block JB0 + l, or JB0 + 3 - l when mirrored, at 4 SA_ blocks) and stores
+// k = 4l + m (store(m, v)).  The inverse loads k = 4l + m, runs the same steps
+// backwards and stores k = l + 4m.
 template <class LOAD, class STORE>
 __device__ __forceinline__ void pass16_fwd(LOAD&& load, STORE&& store, u32 l, const DTw* tw4, u64 SA_, u64 JA, u64 JB0, bool mir) {
     E x[4];
 #pragma unroll
-    for (int m = 0; m < 4; ++m) x[m] = load(l + 4 * m);
+    for (int m = 0; m < 4; ++m) x[m] = load(m);
     {
         const Tri A = tri(tw4, SA_, JA, mir);
         dif4(x[0], x[1], x[2], x[3], A.r1, A.r2, A.r3);
@@ -142,13 +148,13 @@ __device__ __forceinline__ void pass16_fwd(LOAD&& load, STORE&& store, u32 l, co
         dif4(x[0], x[1], x[2], x[3], Bt.r1, Bt.r2, Bt.r3);
     }
 #pragma unroll
-    for (int m = 0; m < 4; ++m) store(4 * l + m, x[m]);
+    for (int m = 0; m < 4; ++m) store(m, x[m]);
 }
 template <class LOAD, class STORE>
 __device__ __forceinline__ void pass16_inv(LOAD&& load, STORE&& store, u32 l, const DTw* tw4, u64 SA_, u64 JA, u64 JB0, bool mir) {
     E x[4];
 #pragma unroll
-    for (int m = 0; m < 4; ++m) x[m] = load(4 * l + m);
+    for (int m = 0; m < 4; ++m) x[m] = load(m);
     {
         const Tri Bt = tri(tw4, 4 * SA_, JB0 + (mir ? 3 - l : l), mir);
         dit4(x[0], x[1], x[2], x[3], Bt.r1, Bt.r2, Bt.r3);
@@ -159,7 +165,7 @@ __device__ __forceinline__ void pass16_inv(LOAD&& load, STORE&& store, u32 l, co
         dit4(x[0], x[1], x[2], x[3], A.r1, A.r2, A.r3);
     }
 #pragma unroll
-    for (int m = 0; m < 4; ++m) store(l + 4 * m, x[m]);
+    for (int m = 0; m < 4; ++m) store(m, x[m]);
 }
 
 }  // namespace
@@ -195,8 +201,9 @@ __global__ void __launch_bounds__(512, (B == 1024) ? 2 : 1) k_rows_q(LargePlan P
         const u32 trow = sl ? t1 : t0;
         const bool mir = general && sl;
         const u32 tsrc = mir ? t0 : trow;
-        pass16_fwd([&](u32 k) { return gload(bf, (u64)trow * B + i + (u64)SA * k); },
-                   [&](u32 k, const E& v) { z.st(sl * B + i + SA * k, v); }, l, bf.tw4, R, tsrc, 4ull * tsrc, mir);
+        const u32 ps = swz(sl * B + i) ^ swz(SA * 4 * l);                    // stores k = 4l + m
+        pass16_fwd([&](int m) { return gload(bf, (u64)trow * B + i + (u64)SA * (l + 4 * m)); },
+                   [&](int m, const E& v) { z.stp(ps ^ swz(SA * m), v); }, l, bf.tw4, R, tsrc, 4ull * tsrc, mir);
     }
     __syncthreads();
     // ---------------- pass B: levels 3-4 ----------------
@@ -208,8 +215,9 @@ __global__ void __launch_bounds__(512, (B == 1024) ? 2 : 1) k_rows_q(LargePlan P
         const u32 tsrc = mir ? t0 : (sl ? t1 : t0);
         const u64 jj = mir ? 15 - jb : jb;
         const u32 base = sl * B + jb * MB + ib;
-        pass16_fwd([&](u32 k) { return z.ld(base + SB * k); }, [&](u32 k, const E& v) { z.st(base + SB * k, v); }, l,
-                   bf.tw4, 16 * R, 16ull * tsrc + jj, 64ull * tsrc + 4 * jj, mir);
+        const u32 pb = swz(base), pl = pb ^ swz(SB * l), p4l = pb ^ swz(SB * 4 * l);
+        pass16_fwd([&](int m) { return z.ldp(pl ^ swz(SB * 4 * m)); }, [&](int m, const E& v) { z.stp(p4l ^ swz(SB * m), v); },
+                   l, bf.tw4, 16 * R, 16ull * tsrc + jj, 64ull * tsrc + 4 * jj, mir);
     }
     __syncthreads();
     // ---------------- tail: last level(s) + centre + first inverse level(s) ----------------
@@ -220,8 +228,9 @@ __global__ void __launch_bounds__(512, (B == 1024) ? 2 : 1) k_rows_q(LargePlan P
         const u32 G = s ? (B / T - 1 - J) : J;
         const u32 ebase = s * B + G * T;
         E x[T];
+        const u32 pe = swz(ebase);                 // ebase is a multiple of T: swz(ebase + b) = pe ^ b
 #pragma unroll
-        for (int b = 0; b < T; ++b) x[b] = z.ld(ebase + b);
+        for (int b = 0; b < T; ++b) x[b] = z.ldp(pe ^ (u32)b);
         const Tri r0 = tri(bf.tw4, S5, (u64)t0 * (B / T) + J, false);
         const Tri r = s ? Tri{mir1(r0.r1), mir2(r0.r2), mir3(r0.r3)} : r0;
         if (T == 4) {
@@ -258,7 +267,7 @@ __global__ void __launch_bounds__(512, (B == 1024) ? 2 : 1) k_rows_q(LargePlan P
             for (int u = 0; u < 2; ++u) dit4(x[u], x[u + 2], x[u + 4], x[u + 6], r.r1, r.r2, r.r3);
         }
 #pragma unroll
-        for (int b = 0; b < T; ++b) z.st(ebase + b, x[b]);
+        for (int b = 0; b < T; ++b) z.stp(pe ^ (u32)b, x[b]);
     } else {
         // rows 0 and 1: each row its own mirror; per-group steps with table twiddles,
         // then per-position centre pairs
@@ -327,8 +336,9 @@ __global__ void __launch_bounds__(512, (B == 1024) ? 2 : 1) k_rows_q(LargePlan P
         const u32 tsrc = mir ? t0 : (sl ? t1 : t0);
         const u64 jj = mir ? 15 - jb : jb;
         const u32 base = sl * B + jb * MB + ib;
-        pass16_inv([&](u32 k) { return z.ld(base + SB * k); }, [&](u32 k, const E& v) { z.st(base + SB * k, v); }, l,
-                   bf.tw4, 16 * R, 16ull * tsrc + jj, 64ull * tsrc + 4 * jj, mir);
+        const u32 pb = swz(base), pl = pb ^ swz(SB * l), p4l = pb ^ swz(SB * 4 * l);
+        pass16_inv([&](int m) { return z.ldp(p4l ^ swz(SB * m)); }, [&](int m, const E& v) { z.stp(pl ^ swz(SB * 4 * m), v); },
+                   l, bf.tw4, 16 * R, 16ull * tsrc + jj, 64ull * tsrc + 4 * jj, mir);
     }
     __syncthreads();
     // ---------------- pass A inverse ----------------
@@ -339,8 +349,9 @@ __global__ void __launch_bounds__(512, (B == 1024) ? 2 : 1) k_rows_q(LargePlan P
         const u32 trow = sl ? t1 : t0;
         const bool mir = general && sl;
         const u32 tsrc = mir ? t0 : trow;
-        pass16_inv([&](u32 k) { return z.ld(sl * B + i + SA * k); },
-                   [&](u32 k, const E& v) { gstore(bf, (u64)trow * B + i + (u64)SA * k, v); }, l, bf.tw4, R, tsrc,
+        const u32 pl = swz(sl * B + i) ^ swz(SA * 4 * l);                    // loads k = 4l + m
+        pass16_inv([&](int m) { return z.ldp(pl ^ swz(SA * m)); },
+                   [&](int m, const E& v) { gstore(bf, (u64)trow * B + i + (u64)SA * (l + 4 * m), v); }, l, bf.tw4, R, tsrc,
                    4ull * tsrc, mir);
     }
 }
