@@ -242,9 +242,12 @@ def run_n22(a, stream) -> dict:
         parity = None
         if done in want:
             parity = "ok" if f"{eng.res64():016x}" == want[done] else "MISMATCH"
+        stages = eng.profile(20)
     return {"p": p, "n": info.n, "ms_per_iter": ms, "iters": steps * ips, "warmup_iters": warm * ips,
-            "plan": {"rows": info.rows, "row_len": info.row_len, "cols_per_cta": info.cols_per_cta},
-            f"res64@{done}": parity}
+            "plan": {"rows": info.rows, "row_len": info.row_len, "cols_per_cta": info.cols_per_cta,
+                     "fused_cols": info.fused_cols},
+            f"res64@{done}": parity,
+            "stages": [{k: st[k] for k in ("name", "ms_per_launch", "launches")} for st in stages]}
 
 
 # ---------------------------------------------------------------- batched
