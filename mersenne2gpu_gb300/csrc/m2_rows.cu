@@ -181,6 +181,10 @@ __global__ void __launch_bounds__(512, 2) k_rows_q(LargePlan P, LargeBufs bf) {
     constexpr int SA = B / 16;                 // pass A stride
     constexpr int MB = B / 16, SB = B / 256;   // pass B block and stride
     constexpr int QIT = (2 * PER * 4) / NT;    // quad-lane roles per thread per pass
+    // launched as a programmatic dependent of the previous column pass: the CTA
+    // may be resident before that grid has finished, and waits here until its
+    // writes are complete and visible
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     extern __shared__ __align__(16) unsigned char smem[];
     const S6 z = make_s6(smem, 2 * B);
     const u32 pi = blockIdx.x, tid = threadIdx.x;
@@ -376,11 +380,21 @@ cudaError_t rows_q_setup(const LargePlan& P) {
 }
 
 cudaError_t launch_rows_q(const LargePlan& P, const LargeBufs& b, cudaStream_t s) {
-    const size_t sm = 24ull * 2 * P.B;
-    if (P.B == 1024) k_rows_q<1024><<<P.R / 2, 512, sm, s>>>(P, b);
-    else if (P.B == 2048) k_rows_q<2048><<<P.R / 2, 512, sm, s>>>(P, b);
-    else return cudaErrorInvalidValue;
-    return cudaGetLastError();
+    // programmatic dependent launch: scheduling overlaps the previous kernel's
+    // tail; the kernel's griddepcontrol.wait orders the data
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(P.R / 2);
+    cfg.blockDim = dim3(512);
+    cfg.dynamicSmemBytes = 24ull * 2 * P.B;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (P.B == 1024) return cudaLaunchKernelEx(&cfg, k_rows_q<1024>, P, b);
+    if (P.B == 2048) return cudaLaunchKernelEx(&cfg, k_rows_q<2048>, P, b);
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace m2k
