@@ -74,28 +74,6 @@ __device__ __forceinline__ Tri tri(const DTw* tw4, u64 S, u64 J) {
     const u64 base = 3 * (S + J);
     return Tri{ldw(tw4, base), ldw(tw4, base + 1), ldw(tw4, base + 2)};
 }
-__device__ __forceinline__ E shfl_xor_e(const E& v, int m) {
-    E r;
-    r.a = __shfl_xor_sync(0xffffffffu, v.a, m);
-    r.b = __shfl_xor_sync(0xffffffffu, v.b, m);
-    r.c = __shfl_xor_sync(0xffffffffu, v.c, m);
-    r.d = __shfl_xor_sync(0xffffffffu, v.d, m);
-    return r;
-}
-__device__ __forceinline__ void quad_transpose(E (&x)[4], u32 l) {
-    {
-        const bool hi = (l & 2u) != 0;
-        const E s0 = hi ? x[0] : x[2], s1 = hi ? x[1] : x[3];
-        const E r0 = shfl_xor_e(s0, 2), r1 = shfl_xor_e(s1, 2);
-        if (hi) { x[0] = r0; x[1] = r1; } else { x[2] = r0; x[3] = r1; }
-    }
-    {
-        const bool hi = (l & 1u) != 0;
-        const E s0 = hi ? x[0] : x[1], s1 = hi ? x[2] : x[3];
-        const E r0 = shfl_xor_e(s0, 1), r1 = shfl_xor_e(s1, 1);
-        if (hi) { x[0] = r0; x[2] = r1; } else { x[1] = r0; x[3] = r1; }
-    }
-}
 
 __device__ __forceinline__ u64 bitpos(u32 p, int ln, u64 j) { return j ? ((((u64)p * j) - 1) >> ln) + 1 : 0; }
 __device__ __forceinline__ u32 width_of(u32 p, int ln, u64 j) { return (u32)(bitpos(p, ln, j + 1) - bitpos(p, ln, j)); }
