@@ -250,6 +250,46 @@ def run_n22(a, stream) -> dict:
             "stages": [{k: st[k] for k in ("name", "ms_per_launch", "launches")} for st in stages]}
 
 
+# ---------------------------------------------------------------- error check
+def run_gec(a, stream) -> dict:
+    """Cost of the Gerbicz error check on the headline exponent: B squarings
+    plain, B squarings with the check product updated at their end, and one
+    verification (B squarings of the product plus one product), wall-clocked
+    on the host after a synchronize; the overhead is amortised over checks
+    every B^2 squarings.  The residue at the end is checked against GMP."""
+    import time
+
+    import mersenne2gpu_gb300 as m2
+    B, blocks = a.gec_block, 4
+    want = {int(k): v for k, v in ((_load_json(GOLDEN_LARGE) or {}).get(str(a.p), {}).get("prp", {})).items()}
+    with m2.Engine(a.p, m2.MODE_PRP, device=stream.device.index or 0, stream=stream.cuda_stream) as eng:
+        eng.iterate(B)                 # warm-up (graph capture, tables)
+        eng.sync()
+        t0 = time.perf_counter()
+        eng.iterate(blocks * B)
+        eng.sync()
+        plain = (time.perf_counter() - t0) / blocks
+        with m2.Gec(eng, B) as g:
+            g.iterate(B)               # warm-up of the second context
+            eng.sync()
+            t0 = time.perf_counter()
+            g.iterate(blocks * B)
+            eng.sync()
+            with_products = (time.perf_counter() - t0) / blocks
+            t0 = time.perf_counter()
+            ok = g.check()
+            check = time.perf_counter() - t0
+            st = g.stats()
+        done = (2 + 2 * blocks) * B
+        parity = None
+        if done in want:
+            parity = "ok" if f"{eng.res64():016x}" == want[done] else "MISMATCH"
+    overhead = (with_products - plain) / plain + check / (B * plain)
+    return {"p": a.p, "block": B, "ms_per_block_plain": plain * 1e3, "ms_per_block_with_product": with_products * 1e3,
+            "ms_per_check": check * 1e3, "check_passed": ok, "updates": st["updates"],
+            "overhead_frac_checks_every_B2": overhead, f"res64@{done}": parity}
+
+
 # ---------------------------------------------------------------- batched
 def run_batched(count: int, plain_sample: int) -> dict:
     import mersenne2gpu_gb300 as m2
@@ -420,6 +460,11 @@ def run_gb300(a, dist: Dist) -> dict | None:
             out["n22"] = run_n22(a, stream)
         except Exception as ex:  # noqa: BLE001
             out["n22"] = {"error": str(ex)}
+    if a.gec and dist.world == 1:
+        try:
+            out["gerbicz"] = run_gec(a, stream)
+        except Exception as ex:  # noqa: BLE001
+            out["gerbicz"] = {"error": str(ex)}
     if a.batch:
         try:
             out["batched"] = run_batched(a.batch_count, a.plain_sample)
@@ -449,6 +494,8 @@ def main() -> int:
     ap.add_argument("--no-n22", dest="n22", action="store_false")
     ap.add_argument("--n22-iters", type=int, default=2500)   # 4 x 2500: checked at GMP's iteration 10000
     ap.add_argument("--n22-steps", type=int, default=2)
+    ap.add_argument("--no-gec", dest="gec", action="store_false")
+    ap.add_argument("--gec-block", type=int, default=1000)
     ap.add_argument("--no-batch", dest="batch", action="store_false")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--plain-sample", type=int, default=8)

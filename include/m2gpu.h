@@ -51,7 +51,8 @@ enum {
     M2_ECUDA = -3,        /* CUDA runtime error (reference: check() -> exit(1), mersenne2_gpu.cpp:3078-3083) */
     M2_ETIMEOUT = -4,     /* a bounded device wait gave up */
     M2_ESTATE = -5,       /* a kernel reported an out-of-range carry / normalization failure */
-    M2_EUNSUPPORTED = -6  /* exponent or option outside what this build supports */
+    M2_EUNSUPPORTED = -6, /* exponent or option outside what this build supports */
+    M2_ECHECK = -7        /* the error check found a wrong state; the context was reset (m2_gec_check) */
 };
 
 typedef struct m2_ctx m2_ctx;
@@ -224,6 +225,51 @@ int m2_carry_normalize(uint32_t p, const int64_t* digits, const int64_t* seg_car
  * state is then meaningless until m2_set_digits reloads it (which also resets
  * the flags).  M2_EUNSUPPORTED when the context has no fused column pass. */
 int m2_test_stall_fused(m2_ctx* ctx);
+
+/* ---------------- Gerbicz error check (PRP) ----------------
+ * A periodic self-check of a PRP chain (M2_MODE_PRP: x <- x^2 from 3), with
+ * rollback to the last verified state.  No reference counterpart: the
+ * reference checks nothing between its start and its final residue
+ * (mersenne2_gpu.cpp:4778-4882).  With x_k the state after k squarings and k0
+ * the last verified iteration, the check product d_t = x_k0 x_(k0+B) ...
+ * x_(k0+tB) is updated every B = `block` squarings, and the chain up to
+ * k0 + tB is correct, but for a chance of about 1 / M_p, when
+ * d_t == x_k0 d_(t-1)^(2^B).  Products a b mod 2^p - 1 are formed as
+ * ((a + b)^2 - (a - b)^2) / 4 from two squarings on a second context of the
+ * same exponent and transform, which also runs the B verification squarings:
+ * every product and square is the engine's own.  The host holds four copies of
+ * the residue (x_k0, d_t, d_(t-1), the last block's state). */
+typedef struct m2_gec m2_gec;
+
+typedef struct {
+    uint32_t verified_iter;  /* k0: iteration of the last verified state */
+    uint32_t block;          /* B */
+    uint64_t updates;        /* products d <- d x taken */
+    uint64_t checks;         /* m2_gec_check calls that verified something */
+    uint64_t failures;       /* of those, the ones that found a wrong state */
+    double seconds;          /* host wall time spent in updates and checks */
+} m2_gec_stats;
+
+/* Starts checking ctx's chain; its current state counts as verified.
+ * M2_EUNSUPPORTED for LL and PRP3 contexts, M2_EINVAL for block = 0. */
+int m2_gec_create(m2_gec** out, m2_ctx* ctx, uint32_t block);
+/* m2_iterate(ctx, k) with the check product updated at every block boundary
+ * passed; returns when the last update is done (the squarings after it are
+ * still queued on ctx's stream). */
+int m2_gec_iterate(m2_gec* g, uint32_t k);
+/* Verifies every squaring since the last verified state: the check-product
+ * relation up to the last block boundary, and the squarings after it by
+ * repeating them on the second context.  M2_OK: the current state is verified
+ * and the check restarts from it.  M2_ECHECK: a mismatch; ctx holds the last
+ * verified state and iteration again.  *verified_iter (may be NULL) receives
+ * the verified iteration either way. */
+int m2_gec_check(m2_gec* g, uint32_t* verified_iter);
+/* The last verified state (n canonical digits) and its iteration: what a
+ * checkpoint file should hold. */
+int m2_gec_verified(m2_gec* g, uint64_t* digits, uint32_t* iteration);
+int m2_gec_stats_get(m2_gec* g, m2_gec_stats* st);
+/* Releases the second context and the host copies; ctx is left as it is. */
+void m2_gec_destroy(m2_gec* g);
 
 /* Digit widths (n bytes) of exponent p, without a device; and log2 n. */
 int m2_layout(uint32_t p, int* ln, uint64_t* n, uint8_t* widths /* may be NULL */);

@@ -27,7 +27,9 @@ EXPORTS = (
     "m2_profile", "m2_launches_for", "m2_measure_mul_peak", "m2_square_noalloc",
     "m2_srv_create", "m2_srv_submit", "m2_srv_step", "m2_srv_poll", "m2_srv_stats_get", "m2_srv_destroy",
     "m2_last_error", "m2_carry_normalize", "m2_batch_tuned", "m2_layout_fields", "m2_test_stall_fused",
+    "m2_gec_create", "m2_gec_iterate", "m2_gec_check", "m2_gec_verified", "m2_gec_stats_get", "m2_gec_destroy",
 )
+E_CHECK = -7   # M2_ECHECK
 
 
 class M2Error(RuntimeError):
@@ -53,6 +55,11 @@ class _Info(ctypes.Structure):
 class _StageTime(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 32), ("ms_per_launch", ctypes.c_double), ("launches", ctypes.c_uint64),
                 ("bytes_per_launch", ctypes.c_uint64), ("iters_per_launch", ctypes.c_uint32)]
+
+
+class _GecStats(ctypes.Structure):
+    _fields_ = [("verified_iter", ctypes.c_uint32), ("block", ctypes.c_uint32), ("updates", ctypes.c_uint64),
+                ("checks", ctypes.c_uint64), ("failures", ctypes.c_uint64), ("seconds", ctypes.c_double)]
 
 
 class _BatchStats(ctypes.Structure):
@@ -94,9 +101,16 @@ def _lib() -> ctypes.CDLL:
         L.m2_test_stall_fused.argtypes = [vp]
         L.m2_batch_tuned.argtypes = [i, i, ctypes.POINTER(i), ctypes.POINTER(ctypes.c_double)]
         L.m2_last_error.argtypes = []
+        L.m2_gec_create.argtypes = [ctypes.POINTER(vp), vp, u32]
+        L.m2_gec_iterate.argtypes = [vp, u32]
+        L.m2_gec_check.argtypes = [vp, ctypes.POINTER(u32)]
+        L.m2_gec_verified.argtypes = [vp, vp, ctypes.POINTER(u32)]
+        L.m2_gec_stats_get.argtypes = [vp, ctypes.POINTER(_GecStats)]
+        L.m2_gec_destroy.argtypes = [vp]
         L.m2_last_error.restype = ctypes.c_char_p
         for name in EXPORTS:
-            if name not in ("m2_destroy", "m2_strerror", "m2_launches_for", "m2_last_error") and not name.startswith("m2_srv"):
+            if name not in ("m2_destroy", "m2_strerror", "m2_launches_for", "m2_last_error", "m2_gec_destroy") \
+                    and not name.startswith("m2_srv"):
                 getattr(L, name).restype = i
         _LIB = L
     return _LIB
@@ -226,6 +240,62 @@ class Engine:
         i = self.info()
         self.iterate(i.total_iters - i.iteration)
         return self.verdict()
+
+
+class Gec:
+    """Gerbicz error check of an Engine's PRP chain (wraps an m2_gec).
+
+    iterate(k) advances the engine by k squarings and updates the check product
+    every `block` squarings; check() verifies everything since the last
+    verified state and returns True, or returns False after putting the engine
+    back to that state (its iteration is then `verified_iter`)."""
+
+    def __init__(self, engine: Engine, block: int):
+        self._L = engine._L
+        self.engine = engine
+        self._h = ctypes.c_void_p()
+        _check(self._L.m2_gec_create(ctypes.byref(self._h), engine._h, block), f"m2_gec_create(block={block})")
+        self.verified_iter = engine.info().iteration
+
+    def close(self) -> None:
+        if self._h:
+            self._L.m2_gec_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def iterate(self, k: int) -> None:
+        _check(self._L.m2_gec_iterate(self._h, k), "m2_gec_iterate")
+
+    def check(self) -> bool:
+        v = ctypes.c_uint32()
+        rc = self._L.m2_gec_check(self._h, ctypes.byref(v))
+        self.verified_iter = v.value
+        if rc == E_CHECK:
+            return False
+        _check(rc, "m2_gec_check")
+        return True
+
+    def verified(self) -> tuple[np.ndarray, int]:
+        d = np.zeros(self.engine.n, dtype=np.uint64)
+        it = ctypes.c_uint32()
+        _check(self._L.m2_gec_verified(self._h, d.ctypes.data, ctypes.byref(it)), "m2_gec_verified")
+        return d, it.value
+
+    def stats(self) -> dict:
+        st = _GecStats()
+        _check(self._L.m2_gec_stats_get(self._h, ctypes.byref(st)), "m2_gec_stats_get")
+        return {k: getattr(st, k) for k, _ in _GecStats._fields_}
 
 
 def measure_mul_peak(device: int = 0) -> float:

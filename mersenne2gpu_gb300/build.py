@@ -20,7 +20,8 @@ LIB = os.path.join(PKG, "libm2gpu.so")
 CLI = os.path.join(PKG, "mersenne2")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["m2_kernels.cu", "m2_rows.cu", "m2_cols.cu", "m2_carry.cu", "m2_api.cu", "m2_peaks.cu", "m2_noalloc.cu"]
+CU_SOURCES = ["m2_kernels.cu", "m2_rows.cu", "m2_cols.cu", "m2_carry.cu", "m2_api.cu", "m2_peaks.cu", "m2_noalloc.cu",
+              "m2_gec.cu"]
 CXX_SOURCES = ["m2_host.cpp"]
 
 
@@ -68,7 +69,7 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src + ".o")
         objs.append(o)
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-I", CSRC, "-c", s, "-o", o]
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I", CSRC, "-c", s, "-o", o]
         if force or _stale(o, [s, *headers]):
             jobs.append(cmd)
     outputs = []

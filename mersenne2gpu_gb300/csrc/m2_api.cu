@@ -1,6 +1,7 @@
 // m2_api.cu -- the C ABI of include/m2gpu.h on top of the kernels.
 #include "../../include/m2gpu.h"
 #include "m2_host.hpp"
+#include "m2_internal.hpp"
 #include "m2_kernels.cuh"
 
 #include <cuda_runtime.h>
@@ -121,6 +122,7 @@ struct m2_ctx {
     int path = M2_PATH_SMALL;
     u32 iteration = 0;
     int device = 0;
+    m2_opts opts{};            // as passed to m2_create, stream cleared
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int span = 0;
@@ -261,6 +263,49 @@ int read_head(m2_ctx* c, std::vector<u64>& head, unsigned& flags) {
 
 }  // namespace
 
+namespace m2i {
+const m2::Layout& layout(const m2_ctx* c) { return c->L; }
+m2_opts creation_opts(const m2_ctx* c) { return c->opts; }
+cudaStream_t stream(const m2_ctx* c) { return c->stream; }
+
+int canonical(m2_ctx* c, const unsigned long long** out) {
+    if (cudaSetDevice(c->device) != cudaSuccess) return M2_ECUDA;
+    m2k::NormArgs a;
+    const int rc = device_canonical(c, a);
+    if (!rc) *out = c->d_canon;
+    return rc;
+}
+
+int raw_state(m2_ctx* c, long long** digits) {
+    if (cudaSetDevice(c->device) != cudaSuccess) return M2_ECUDA;
+    cudaError_t e = cudaSuccess;
+    if (c->path == M2_PATH_LARGE) e = cudaMemsetAsync(c->d_carries, 0, sizeof(i64) * (size_t)c->plan.R * c->plan.G, c->stream);
+    if (e != cudaSuccess) return fail_cuda("state reset", e);
+    *digits = c->d_digits;
+    return M2_OK;
+}
+
+int canon_buffer(m2_ctx* c, unsigned long long** buf) {
+    int rc;
+    if (!c->d_canon && (rc = dalloc(c, &c->d_canon, c->L.n * sizeof(u64)))) return rc;
+    if (!c->d_norm && (rc = dalloc(c, (char**)&c->d_norm, m2k::norm_scratch_bytes(c->L.n)))) return rc;
+    *buf = c->d_canon;
+    return M2_OK;
+}
+
+int load_canon(m2_ctx* c, uint32_t iteration) {
+    if (cudaSetDevice(c->device) != cudaSuccess) return M2_ECUDA;
+    cudaError_t e = m2k::launch_balance(c->d_canon, c->d_digits, c->L.p, c->L.ln, c->L.n, nullptr, c->stream);
+    if (e == cudaSuccess && c->path == M2_PATH_LARGE)
+        e = cudaMemsetAsync(c->d_carries, 0, sizeof(i64) * (size_t)c->plan.R * c->plan.G, c->stream);
+    if (e == cudaSuccess && c->d_flags) e = cudaMemsetAsync(c->d_flags, 0, sizeof(unsigned) * c->plan.G, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream);
+    if (e != cudaSuccess) return fail_cuda("state load", e);
+    c->iteration = iteration;
+    return M2_OK;
+}
+}  // namespace m2i
+
 extern "C" {
 
 const char* m2_last_error(void) { return g_last_error; }
@@ -274,6 +319,7 @@ const char* m2_strerror(int code) {
         case M2_ETIMEOUT: return "device wait timed out";
         case M2_ESTATE: return "device reported an out-of-range carry";
         case M2_EUNSUPPORTED: return "unsupported exponent or option";
+        case M2_ECHECK: return "error check failed; state reset to the last verified one";
         default: return "unknown error";
     }
 }
@@ -305,6 +351,8 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
     c->gf61 = gf61;
     c->mode = mode;
     c->device = o.device;
+    c->opts = o;
+    c->opts.stream = nullptr;
     if (cudaSetDevice(o.device) != cudaSuccess) { cudaGetLastError(); return M2_EINVAL; }
     c->span = m2::carry_span(c->L);
     const u64 h = c->L.h;

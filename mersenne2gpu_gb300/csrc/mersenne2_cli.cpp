@@ -14,8 +14,12 @@
 // (GF(P61^2) alone with that prototype's size rule), --res64
 // (append the 64-bit residue to every progress line), --path small|large,
 // --checkpoint FILE / --resume FILE (state files: magic, p, mode, iteration, n,
-// canonical digits, FNV-1a checksum; written through a temporary file), and
-// a final "res64=" line.
+// canonical digits, FNV-1a checksum; written through a temporary file),
+// --gerbicz B (PRP only: Gerbicz error check with block B, verified every B^2
+// squarings and at the end, rolling back to the last verified state on a
+// mismatch; checkpoints then hold verified states only), --debug-gec-corrupt
+// ITER (flips one bit of the state once, at the first report point at or after
+// ITER: a host-side fault for testing the check), and a final "res64=" line.
 #include "m2gpu.h"
 
 #include <csignal>
@@ -41,7 +45,8 @@ namespace {
 const char* kUsage =
     " <p> [ll|prp] [report_every] [-d device_id] [-R report_seconds] [-W fft_wg] [-CW carry_wg] [-B carry_pairs] "
     "[-LS local_stage_cap] [-N max_iters] [--show-defaults] [--enable-chunk64] [--debug-plan] [--debug-stage-selftest] "
-    "[--debug-cppint-every N] [--debug-cppint-max-iter N]\n";
+    "[--debug-cppint-every N] [--debug-cppint-max-iter N] [--res64] [--path small|large] [--gf61] [--checkpoint FILE] "
+    "[--resume FILE] [--gerbicz B] [--debug-gec-corrupt ITER]\n";
 
 void usage(const char* argv0) { std::cerr << "Usage: " << argv0 << kUsage; }
 
@@ -120,6 +125,7 @@ int main(int argc, char* argv[]) {
     int path = M2_PATH_AUTO;
     int fields = M2_FIELDS_DUAL;
     std::string checkpoint, resume;
+    uint32_t gec_block = 0u, corrupt_at = 0u;
 
     auto need = [&](int& i, const char* what) -> const char* {
         if (i + 1 >= argc) { std::cerr << "Missing " << what << "\n"; std::exit(1); }
@@ -166,6 +172,11 @@ int main(int argc, char* argv[]) {
             checkpoint = need(i, "file after --checkpoint");
         } else if (arg == "--resume") {
             resume = need(i, "file after --resume");
+        } else if (arg == "--gerbicz") {
+            gec_block = (uint32_t)std::strtoul(need(i, "block length after --gerbicz"), nullptr, 10);
+            if (gec_block == 0u) { std::cerr << "--gerbicz needs a block length >= 1\n"; return 1; }
+        } else if (arg == "--debug-gec-corrupt") {
+            corrupt_at = (uint32_t)std::strtoul(need(i, "iteration after --debug-gec-corrupt"), nullptr, 10);
         } else if (!report_every_set) {
             report_every = (uint32_t)std::strtoul(arg.c_str(), nullptr, 10);
             report_every_set = true;
@@ -182,6 +193,7 @@ int main(int argc, char* argv[]) {
         std::cout << "debug_cppint disabled at runtime; exact residues are verified by the test suite\n";
     }
     if (p < 3) { std::cerr << "exponent must be >= 3\n"; return 1; }
+    if (gec_block && mode != M2_MODE_PRP) { std::cerr << "--gerbicz applies to prp only\n"; return 1; }
 
     int ln = 0;
     uint64_t n = 0;
@@ -272,6 +284,14 @@ int main(int argc, char* argv[]) {
         std::cout << "resumed at iter " << iter << "\n";
     }
 
+    m2_gec* gec = nullptr;
+    if (gec_block && (rc = m2_gec_create(&gec, ctx, gec_block))) { m2_destroy(ctx); return fail(rc, "m2_gec_create"); }
+    auto finish = [&](int code) {
+        m2_gec_destroy(gec);
+        m2_destroy(ctx);
+        return code;
+    };
+
     (void)report_seconds;   // parsed as in the reference, where every report is forced (mersenne2_gpu.cpp:4810, 4852)
     const auto t0 = std::chrono::steady_clock::now();
     const uint32_t iter0 = iter;
@@ -294,31 +314,60 @@ int main(int argc, char* argv[]) {
         std::cout.unsetf(std::ios::fixed);
         if (!checkpoint.empty()) {
             std::vector<uint64_t> d(n);
-            if ((r = m2_get_digits(ctx, d.data()))) return r;
-            if (!save_state(checkpoint, p, mode, it, d)) std::cerr << "warning: cannot write " << checkpoint << "\n";
+            uint32_t at = it;
+            if ((r = gec ? m2_gec_verified(gec, d.data(), &at) : m2_get_digits(ctx, d.data()))) return r;
+            if (!save_state(checkpoint, p, mode, at, d)) std::cerr << "warning: cannot write " << checkpoint << "\n";
         }
         return 0;
     };
     if (max_iters_override != 0u) std::cout << "benchmark_iters=" << total_iters << "\n";
     uint32_t batch = std::max<uint32_t>(1u, report_every != 0u ? report_every : 1000u);
-    if ((rc = report(iter))) { m2_destroy(ctx); return fail(rc, "report"); }
+    if ((rc = report(iter))) return finish(fail(rc, "report"));
     std::signal(SIGINT, on_sigint);
+    const uint64_t check_every = (uint64_t)gec_block * gec_block;
+    uint32_t last_check = iter, failed_in_row = 0;
+    bool corrupted = false;
     while (iter < total_iters) {
         const uint32_t k = std::min(batch, total_iters - iter);
-        if ((rc = m2_iterate(ctx, k))) { m2_destroy(ctx); return fail(rc, "m2_iterate"); }
+        if ((rc = gec ? m2_gec_iterate(gec, k) : m2_iterate(ctx, k))) return finish(fail(rc, "m2_iterate"));
         iter += k;
-        if ((rc = report(iter))) { m2_destroy(ctx); return fail(rc, "report"); }
+        if (corrupt_at && !corrupted && iter >= corrupt_at) {
+            std::vector<uint64_t> d(n);
+            if ((rc = m2_get_digits(ctx, d.data()))) return finish(fail(rc, "m2_get_digits"));
+            d[0] ^= 1u;   // digit 0 is ceil(p / n) >= 1 bits wide
+            if ((rc = m2_set_digits(ctx, d.data(), iter))) return finish(fail(rc, "m2_set_digits"));
+            corrupted = true;
+            std::cout << "debug: one bit of the state flipped at iter " << iter << "\n";
+        }
+        if (gec && (iter - last_check >= check_every || iter == total_iters)) {
+            uint32_t verified = 0;
+            rc = m2_gec_check(gec, &verified);
+            if (rc == M2_ECHECK) {
+                std::cout << "gerbicz check failed at iter " << iter << ", back to iter " << verified << "\n" << std::flush;
+                iter = last_check = verified;
+                if (++failed_in_row >= 3) {
+                    std::cerr << "gerbicz check failed 3 times in a row from iter " << verified << "\n";
+                    return finish(1);
+                }
+            } else if (rc) {
+                return finish(fail(rc, "m2_gec_check"));
+            } else {
+                failed_in_row = 0;
+                last_check = iter;
+                std::cout << "gerbicz check passed at iter " << iter << "\n";
+            }
+        }
+        if ((rc = report(iter))) return finish(fail(rc, "report"));
         if (g_stop && iter < total_iters) {
             std::cout << "interrupted at iter " << iter;
             if (!checkpoint.empty()) std::cout << ", state saved to " << checkpoint;
             std::cout << "\n" << std::flush;
-            m2_destroy(ctx);
-            return 130;
+            return finish(130);
         }
     }
     int prime = 0;
     uint64_t r64 = 0;
-    if ((rc = m2_verdict(ctx, &prime)) || (rc = m2_res64(ctx, &r64))) { m2_destroy(ctx); return fail(rc, "verdict"); }
+    if ((rc = m2_verdict(ctx, &prime)) || (rc = m2_res64(ctx, &r64))) return finish(fail(rc, "verdict"));
     const double elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     const double itps = elapsed > 0.0 ? (iter - iter0) / elapsed : 0.0;
     std::cout << "2^" << p << " - 1 is "
@@ -326,6 +375,11 @@ int main(int argc, char* argv[]) {
               << ", elapsed " << std::fixed << std::setprecision(2) << elapsed << " s, it/s " << std::setprecision(1)
               << itps << "\n";
     std::cout << "res64=" << hex64(r64) << "\n";
-    m2_destroy(ctx);
-    return 0;
+    if (gec) {
+        m2_gec_stats st{};
+        m2_gec_stats_get(gec, &st);
+        std::cout << "gerbicz block=" << st.block << ", updates=" << st.updates << ", checks=" << st.checks
+                  << ", failures=" << st.failures << ", check time " << std::setprecision(2) << st.seconds << " s\n";
+    }
+    return finish(0);
 }
