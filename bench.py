@@ -492,8 +492,8 @@ def main() -> int:
     ap.add_argument("--cpu-iters", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-n22", dest="n22", action="store_false")
-    ap.add_argument("--n22-iters", type=int, default=2500)   # 4 x 2500: checked at GMP's iteration 10000
-    ap.add_argument("--n22-steps", type=int, default=2)
+    ap.add_argument("--n22-iters", type=int, default=2500)
+    ap.add_argument("--n22-steps", type=int, default=6)   # (2 + 6) x 2500: checked at GMP's iteration 20000
     ap.add_argument("--no-gec", dest="gec", action="store_false")
     ap.add_argument("--gec-block", type=int, default=1000)
     ap.add_argument("--no-batch", dest="batch", action="store_false")

@@ -237,8 +237,10 @@ int m2_test_stall_fused(m2_ctx* ctx);
  * d_t == x_k0 d_(t-1)^(2^B).  Products a b mod 2^p - 1 are formed as
  * ((a + b)^2 - (a - b)^2) / 4 from two squarings on a second context of the
  * same exponent and transform, which also runs the B verification squarings:
- * every product and square is the engine's own.  The host holds four copies of
- * the residue (x_k0, d_t, d_(t-1), the last block's state). */
+ * every product and square is the engine's own.  Device memory: six vectors
+ * of n words plus the second context.  While a check is attached, every
+ * squaring of ctx goes through m2_gec_iterate (m2_set_digits on ctx is
+ * allowed: a state changed behind the check's back fails the next check). */
 typedef struct m2_gec m2_gec;
 
 typedef struct {

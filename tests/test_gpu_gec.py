@@ -82,6 +82,17 @@ def test_gec_catches_flip_three_pass_n2_21(m2):
         assert f"{e.res64():016x}" == want
 
 
+def test_gec_catches_flip_n2_22_separate_column_passes(m2):
+    """p = 115640321 (n = 2^22: separate inverse and forward column passes):
+    B = 100, checks every 300 squarings, one bit flipped at 350."""
+    want = _golden("large.json")["115640321"]["prp"]["1000"]
+    with m2.Engine(115640321, "prp") as e, m2.Gec(e, 100) as g:
+        assert e.info().path == m2.PATH_LARGE and e.info().n == 1 << 22
+        log = _run_checked(g, 1000, 300, flip_at=350, chunk=50)
+        assert [ok for _, ok in log] == [True, False, True, True, True], log
+        assert f"{e.res64():016x}" == want
+
+
 def test_gec_tail_only_and_mid_size(m2):
     """Checks inside the first block (nothing but repeated squarings to
     compare) on p = 132049 (n = 4096, three-pass path), against GMP."""
