@@ -184,6 +184,65 @@ def reference_sample(p: int, iters: int) -> tuple[float, int, float]:
     return dt / iters * 1e3, oracle.RefKernels.threads(), setup
 
 
+def reference_single_thread(p: int, iters: int) -> float:
+    """ms per iteration of the reference's own kernels on one host thread."""
+    import oracle
+    all_threads = oracle.RefKernels.threads()
+    r = oracle.RefKernels(p, oracle.PRP)
+    try:
+        oracle.RefKernels.set_threads(1)
+        r.iterate(1)
+        t0 = time.perf_counter()
+        r.iterate(iters)
+        return (time.perf_counter() - t0) / iters * 1e3
+    finally:
+        oracle.RefKernels.set_threads(all_threads)
+
+
+def gmp_sample(p: int, iters: int) -> dict:
+    """Single-thread GMP (mpz_mul, then the fold mod 2^p - 1) on a full-size
+    residue: a secondary CPU row beside the reference's own kernels."""
+    import ctypes
+    import ctypes.util
+    G = ctypes.CDLL(ctypes.util.find_library("gmp") or "libgmp.so.10")
+
+    class Z(ctypes.Structure):
+        _fields_ = [("alloc", ctypes.c_int), ("size", ctypes.c_int), ("d", ctypes.c_void_p)]
+
+    x, m, hi = Z(), Z(), Z()
+    bx, bm, bh = ctypes.byref(x), ctypes.byref(m), ctypes.byref(hi)
+    ul = ctypes.c_ulong
+    for z in (bx, bm, bh):
+        G.__gmpz_init(z)
+    try:
+        G.__gmpz_ui_pow_ui(bm, ul(2), ul(p))
+        G.__gmpz_sub_ui(bm, bm, ul(1))            # M_p
+        G.__gmpz_tdiv_q_ui(bx, bm, ul(3))         # a full-size residue (M_p - 12345 would square to a tiny one)
+
+        def square():
+            G.__gmpz_mul(bx, bx, bx)
+            G.__gmpz_tdiv_q_2exp(bh, bx, ul(p))
+            G.__gmpz_tdiv_r_2exp(bx, bx, ul(p))
+            G.__gmpz_add(bx, bx, bh)
+            if G.__gmpz_cmp(bx, bm) >= 0:
+                G.__gmpz_sub(bx, bx, bm)
+
+        square()
+        t0 = time.perf_counter()
+        for _ in range(iters):
+            square()
+        ms = (time.perf_counter() - t0) / iters * 1e3
+        G.__gmpz_sizeinbase.restype = ctypes.c_size_t
+        bits = int(G.__gmpz_sizeinbase(bx, 2))
+        if bits < p - 64:
+            raise RuntimeError(f"residue shrank to {bits} bits")
+    finally:
+        for z in (bx, bm, bh):
+            G.__gmpz_clear(z)
+    return {"value": ms, "unit": "ms/iter", "cores": 1, "kind": "gmp",
+            "sample": f"{iters} squarings mod 2^{p}-1 of a full-size residue with libgmp mpz_mul (one thread)"}
+
+
 def run_reference(a, dist: Dist) -> dict | None:
     if dist.rank != 0:
         return None
@@ -452,9 +511,20 @@ def run_gb300(a, dist: Dist) -> dict | None:
             out["cpu_baseline"] = {"value": ms, "unit": "ms/iter", "cores": thr, "kind": "reference",
                                    "sample": f"{a.cpu_iters} squarings of p={a.p} (n=2^21) through the reference's "
                                              f"own kernels on the host cores (table setup {setup:.1f} s untimed)"}
+            try:
+                out["cpu_baseline"]["single_thread"] = {
+                    "value": reference_single_thread(a.p, 2), "unit": "ms/iter", "cores": 1, "kind": "reference",
+                    "sample": f"2 squarings of p={a.p} through the reference's own kernels on one host thread"}
+            except Exception as ex:  # noqa: BLE001
+                out["cpu_baseline"]["single_thread"] = {"value": None, "sample": f"unavailable: {ex}"}
         except Exception as ex:  # noqa: BLE001
             out["cpu_baseline"] = {"value": None, "unit": "ms/iter", "cores": 0, "kind": "reference",
                                    "sample": f"unavailable: {ex}"}
+    if a.cpu_baseline and dist.world == 1 and isinstance(out.get("cpu_baseline"), dict):
+        try:
+            out["cpu_baseline"]["gmp_single_thread"] = gmp_sample(a.p, 3)
+        except Exception as ex:  # noqa: BLE001
+            out["cpu_baseline"]["gmp_single_thread"] = {"value": None, "sample": f"unavailable: {ex}"}
     if a.n22 and dist.world == 1:
         try:
             out["n22"] = run_n22(a, stream)

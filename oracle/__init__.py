@@ -168,6 +168,13 @@ class RefKernels:
         L = _ref_lib()
         return int(L.ref_threads()) if L is not None else 0
 
+    @staticmethod
+    def set_threads(n: int) -> None:
+        """Threads of the work-item loops from now on (OpenMP)."""
+        L = _ref_lib()
+        if L is not None:
+            L.ref_set_threads(ctypes.c_int(n))
+
 
 def python_chain(p: int, mode: int, iters: int, x0: int | None = None) -> int:
     """Exact x after `iters` steps (Python integers); small p only."""

@@ -117,6 +117,16 @@ int ref_threads(void) {
 #endif
 }
 
+// threads of the work-item loops from now on (n >= 1): the single-thread row
+// of the CPU baseline
+void ref_set_threads(int n) {
+#ifdef _OPENMP
+    if (n >= 1) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
 // k squarings through M2's generic kernel sequence (M2:4327-4765).
 void ref_iterate(void* hp, uint32_t k) {
     RefCtx* c = static_cast<RefCtx*>(hp);
