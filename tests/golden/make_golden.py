@@ -29,6 +29,7 @@ sys.path.insert(0, ROOT)
 SMALL_P = [3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 61, 89, 107, 127, 521, 607, 1279, 2203, 2281, 3217, 4253, 4423,
            9689, 9941, 11213, 19937, 21701, 23209, 44497, 8191, 8209, 10007, 30011]
 LARGE = {57885161: [1000, 10000, 20000, 21000], 115640321: [1000, 10000, 20000, 21000]}
+LARGE_LL = {57885161: [1000], 115640321: [1000]}   # the LL -2 step through the n = 2^21 / 2^22 kernels
 
 
 def gmp_bin(cache: str) -> str:
@@ -122,10 +123,11 @@ def make_mid(cache: str, jobs: int) -> dict:
 
 def make_large(cache: str, jobs: int) -> dict:
     out = {}
+    runs = [(p, "prp", c) for p, c in LARGE.items()] + [(p, "ll", c) for p, c in LARGE_LL.items()]
     with cf.ThreadPoolExecutor(jobs) as ex:
-        futs = {p: ex.submit(gmp_run, cache, p, "prp", max(c), ",".join(map(str, c))) for p, c in LARGE.items()}
-    for p, fu in futs.items():
-        out[str(p)] = {"prp": {str(k): v[0] for k, v in sorted(fu.result().items())}}
+        futs = {(p, m): ex.submit(gmp_run, cache, p, m, max(c), ",".join(map(str, c))) for p, m, c in runs}
+    for (p, m), fu in futs.items():
+        out.setdefault(str(p), {})[m] = {str(k): v[0] for k, v in sorted(fu.result().items())}
     return out
 
 

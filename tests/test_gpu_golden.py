@@ -77,13 +77,13 @@ def test_config2_mid_exponents(m2):
 def test_config3_large_checkpoints(m2):
     g = _load("large.json")
     for p, rec in g.items():
-        cps = sorted(int(k) for k in rec["prp"])
-        with m2.Engine(int(p), MODES["prp"]) as e:
-            done = 0
-            for it in cps:
-                e.iterate(it - done)
-                done = it
-                assert f"{e.res64():016x}" == rec["prp"][str(it)], (p, it)
+        for mode, cp in rec.items():
+            with m2.Engine(int(p), MODES[mode]) as e:
+                done = 0
+                for it in sorted(int(k) for k in cp):
+                    e.iterate(it - done)
+                    done = it
+                    assert f"{e.res64():016x}" == cp[str(it)], (p, mode, it)
 
 
 def test_config4_batched_golden_and_plain(m2):
