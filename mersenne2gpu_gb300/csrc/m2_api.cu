@@ -165,6 +165,10 @@ template <class T> int dalloc(m2_ctx* c, T** p, size_t bytes) {
     return M2_OK;
 }
 
+// the fused column kernel's G epoch flags followed by its 64-bit ticket
+// counter (G is even, so the counter is 8-byte aligned)
+size_t flags_bytes(const m2k::LargePlan& P) { return sizeof(unsigned) * ((size_t)P.G + 2); }
+
 bool plan_large(const m2::Layout& L, int span, u32 carry_pairs, m2k::LargePlan& P) {
     const int Lh = L.ln - 1;
     if (Lh < 6) return false;
@@ -226,7 +230,7 @@ int upload_state(m2_ctx* c, const std::vector<u64>& canon) {
     cudaError_t e = cudaMemcpyAsync(c->d_digits, bal.data(), bal.size() * sizeof(i64), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess && c->path == M2_PATH_LARGE)
         e = cudaMemsetAsync(c->d_carries, 0, sizeof(i64) * (size_t)c->plan.R * c->plan.G, c->stream);
-    if (e == cudaSuccess && c->d_flags) e = cudaMemsetAsync(c->d_flags, 0, sizeof(unsigned) * c->plan.G, c->stream);
+    if (e == cudaSuccess && c->d_flags) e = cudaMemsetAsync(c->d_flags, 0, flags_bytes(c->plan), c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     return cuda_err(e);
 }
@@ -298,7 +302,7 @@ int load_canon(m2_ctx* c, uint32_t iteration) {
     cudaError_t e = m2k::launch_balance(c->d_canon, c->d_digits, c->L.p, c->L.ln, c->L.n, nullptr, c->stream);
     if (e == cudaSuccess && c->path == M2_PATH_LARGE)
         e = cudaMemsetAsync(c->d_carries, 0, sizeof(i64) * (size_t)c->plan.R * c->plan.G, c->stream);
-    if (e == cudaSuccess && c->d_flags) e = cudaMemsetAsync(c->d_flags, 0, sizeof(unsigned) * c->plan.G, c->stream);
+    if (e == cudaSuccess && c->d_flags) e = cudaMemsetAsync(c->d_flags, 0, flags_bytes(c->plan), c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream);
     if (e != cudaSuccess) return fail_cuda("state load", e);
     c->iteration = iteration;
@@ -403,7 +407,7 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
         raw->plan.mode = mode;
         if ((rc = dalloc(raw, &raw->d_carries, sizeof(i64) * (size_t)P.R * P.G)) ||
             (rc = dalloc(raw, &raw->d_za, sizeof(ulonglong2) * h)) || (rc = dalloc(raw, &raw->d_zb, sizeof(uint2) * h)) ||
-            (rc = dalloc(raw, &raw->d_flags, sizeof(unsigned) * P.G))) {
+            (rc = dalloc(raw, &raw->d_flags, flags_bytes(P)))) {
             m2_destroy(c.release());
             return rc;
         }
@@ -411,6 +415,8 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
                                    raw->tw.tw4, raw->tw.tc, raw->d_status, raw->d_flags};
         if (m2k::large_setup(P) != cudaSuccess) { m2_destroy(c.release()); return M2_EUNSUPPORTED; }
         raw->fused = m2k::cols_mid_supported(P);
+        raw->plan.mid_tickets = (raw->fused && !m2k::cols_mid_cooperative(P)) ? 1u : 0u;
+        raw->bufs.ticket = reinterpret_cast<unsigned long long*>(raw->d_flags + P.G);
     }
     raw->bytes += raw->tw.bytes;
     if ((rc = upload_state(raw, m2::digits_of_small(raw->L, mode == M2_MODE_LL ? 4 : 3)))) { m2_destroy(c.release()); return rc; }
@@ -472,7 +478,7 @@ int m2_set_digits(m2_ctx* c, const uint64_t* digits, uint32_t iteration) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess && c->path == M2_PATH_LARGE)
         e = cudaMemsetAsync(c->d_carries, 0, sizeof(i64) * (size_t)c->plan.R * c->plan.G, c->stream);
-    if (e == cudaSuccess && c->d_flags) e = cudaMemsetAsync(c->d_flags, 0, sizeof(unsigned) * c->plan.G, c->stream);
+    if (e == cudaSuccess && c->d_flags) e = cudaMemsetAsync(c->d_flags, 0, flags_bytes(c->plan), c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return fail_cuda("state upload", e);

@@ -401,15 +401,33 @@ __global__ void __launch_bounds__(ColShape<CR>::CNT, 65536 / (64 * ColShape<CR>:
 // before).  Every CTA publishes its carries, raises its flag to this launch's
 // epoch (one more than its value at entry; every launch raises every flag
 // once, so all flags are equal between launches) and waits, bounded, for its
-// predecessor's flag.  Launched cooperatively, so all G CTAs are resident and
-// the waits end; a wait that runs out sets ST_WAIT_TIMEOUT and the CTA goes on.
-template <int CR>
+// predecessor's flag; a wait that runs out sets ST_WAIT_TIMEOUT and the CTA
+// goes on.
+//  * TK = false: launched cooperatively, all G CTAs resident, CTA g is group g.
+//  * TK = true: G CTAs that need not all fit at once (G = 512 at n = 2^22).
+//    Each CTA takes its group from a 64-bit ticket counter in arrival order
+//    (ticket t of a launch is group t mod G: every launch draws exactly G).
+//    The CTA of group g >= 1 then waits only on a CTA that arrived before it,
+//    is resident, and publishes before it waits itself; only group 0 waits on
+//    a later arrival (group G-1), which gets a slot as the others finish.
+template <int CR, bool TK>
 __global__ void __launch_bounds__(ColShape<CR>::CNT, 65536 / (64 * ColShape<CR>::CNT)) k_cols_mid_q(LargePlan P, LargeBufs bf) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned s_epoch;
     const S6c z = make_s6c(smem, CR * CC);
-    const u32 g = blockIdx.x, G = P.G;
-    if (threadIdx.x == 0) s_epoch = bf.flags[g] + 1u;
+    const u32 G = P.G;
+    u32 g = blockIdx.x;
+    if (TK) {
+        __shared__ unsigned s_g;
+        if (threadIdx.x == 0) {
+            s_g = (unsigned)(atomicAdd(bf.ticket, 1ull) % G);
+            s_epoch = bf.flags[s_g] + 1u;
+        }
+        __syncthreads();
+        g = s_g;
+    } else if (threadIdx.x == 0) {
+        s_epoch = bf.flags[g] + 1u;
+    }
     inv_passes<CR>(z, P, bf, g);
     __syncthreads();
     inv_row_stage<CR, true>(z, P, bf, g);
@@ -444,10 +462,12 @@ cudaError_t setup_shape() {
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(k_cols_fwd_q<CR>, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
     if ((e = cudaFuncSetAttribute(k_cols_inv_q<CR>, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
-    if ((e = cudaFuncSetAttribute(k_cols_mid_q<CR>, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
+    if ((e = cudaFuncSetAttribute(k_cols_mid_q<CR, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
+    if ((e = cudaFuncSetAttribute(k_cols_mid_q<CR, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100))) return e;
+    if ((e = cudaFuncSetAttribute(k_cols_mid_q<CR, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
     if ((e = cudaFuncSetAttribute(k_cols_fwd_q<CR>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
     if ((e = cudaFuncSetAttribute(k_cols_inv_q<CR>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm))) return e;
-    return cudaFuncSetAttribute(k_cols_mid_q<CR>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    return cudaFuncSetAttribute(k_cols_mid_q<CR, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
 }
 template <int CR>
 bool mid_fits(const LargePlan& P) {
@@ -455,7 +475,7 @@ bool mid_fits(const LargePlan& P) {
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return false;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return false;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cols_mid_q<CR>, ColShape<CR>::CNT, 24ull * CR * CC) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cols_mid_q<CR, false>, ColShape<CR>::CNT, 24ull * CR * CC) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
@@ -463,6 +483,10 @@ bool mid_fits(const LargePlan& P) {
 }
 template <int CR>
 cudaError_t launch_mid(const LargePlan& P, const LargeBufs& b, cudaStream_t s) {
+    if (P.mid_tickets) {
+        k_cols_mid_q<CR, true><<<P.G, ColShape<CR>::CNT, 24ull * CR * CC, s>>>(P, b);
+        return cudaGetLastError();
+    }
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(P.G);
     cfg.blockDim = dim3(ColShape<CR>::CNT);
@@ -473,14 +497,17 @@ cudaError_t launch_mid(const LargePlan& P, const LargeBufs& b, cudaStream_t s) {
     at[0].val.cooperative = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_cols_mid_q<CR>, P, b);
+    return cudaLaunchKernelEx(&cfg, k_cols_mid_q<CR, false>, P, b);
 }
 }  // namespace
 
 cudaError_t cols_q_setup(const LargePlan& P) { return P.R == 1024u ? setup_shape<1024>() : setup_shape<256>(); }
 
-// true when all G CTAs of the fused kernel fit on the device at once
-bool cols_mid_supported(const LargePlan& P) {
+// the fused kernel serves every plan of the quad-shuffle column kernels: with
+// a cooperative launch when all G CTAs fit on the device at once, else with
+// groups by arrival ticket
+bool cols_mid_supported(const LargePlan& P) { return cols_q_supported(P); }
+bool cols_mid_cooperative(const LargePlan& P) {
     if (!cols_q_supported(P)) return false;
     return P.R == 1024u ? mid_fits<1024>(P) : mid_fits<256>(P);
 }

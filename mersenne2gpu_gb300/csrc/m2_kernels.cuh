@@ -37,6 +37,7 @@ struct LargePlan {
     int span;
     unsigned int p;
     int mode;
+    unsigned int mid_tickets;  // fused column kernel: 0 = cooperative (CTA index = group), 1 = groups by arrival ticket
 };
 
 struct LargeBufs {
@@ -49,7 +50,8 @@ struct LargeBufs {
     const DTw* tw4;
     const DTw* tc;
     int* status;
-    unsigned int* flags;      // G epoch flags of the fused column kernel (zero-initialised)
+    unsigned int* flags;      // G epoch flags of the fused column kernel, then its 64-bit ticket counter (zero-initialised)
+    unsigned long long* ticket;
 };
 
 size_t small_smem_bytes(unsigned int h, int threads);
@@ -77,7 +79,8 @@ cudaError_t launch_rows_q(const LargePlan& P, const LargeBufs& b, cudaStream_t s
 bool cols_q_supported(const LargePlan& P);
 cudaError_t cols_q_setup(const LargePlan& P);
 cudaError_t launch_cols_q(const LargePlan& P, const LargeBufs& b, bool inverse, cudaStream_t s);
-bool cols_mid_supported(const LargePlan& P);   // all G CTAs co-resident (cooperative launch)
+bool cols_mid_supported(const LargePlan& P);     // the fused column kernel serves this plan
+bool cols_mid_cooperative(const LargePlan& P);   // ... with all G CTAs co-resident (cooperative launch)
 cudaError_t launch_cols_mid(const LargePlan& P, const LargeBufs& b, cudaStream_t s);
 cudaError_t launch_large_stage(const LargePlan& P, const LargeBufs& b, int stage, cudaStream_t s);
 const char* large_stage_name(int stage);

@@ -252,7 +252,7 @@ int main(int argc, char* argv[]) {
             // first squaring: fwd, rows; every further one: mid, rows; after the last: inv
             const uint32_t gcol = info.row_len / info.cols_per_cta;
             std::cout << "iter_plan_steps=2 (the first squaring starts with k_cols_fwd, the last ends with k_cols_inv)\n"
-                      << "  [0] k_cols_mid gs=" << gcol * 512 << " ls=512 (cooperative)\n"
+                      << "  [0] k_cols_mid gs=" << gcol * 512 << " ls=512 (fused inverse + next forward column pass)\n"
                       << "  [1] k_rows gs=" << (info.rows / 2) * 512 << " ls=512\n"
                       << "  [pre] k_cols_fwd gs=" << gcol * 512 << " ls=512\n"
                       << "  [post] k_cols_inv gs=" << gcol * 512 << " ls=512\n";

@@ -82,9 +82,9 @@ def test_gec_catches_flip_three_pass_n2_21(m2):
         assert f"{e.res64():016x}" == want
 
 
-def test_gec_catches_flip_n2_22_separate_column_passes(m2):
-    """p = 115640321 (n = 2^22: separate inverse and forward column passes):
-    B = 100, checks every 300 squarings, one bit flipped at 350."""
+def test_gec_catches_flip_n2_22(m2):
+    """p = 115640321 (n = 2^22: the fused column pass with groups taken by
+    arrival ticket): B = 100, checks every 300 squarings, one bit flipped at 350."""
     want = _golden("large.json")["115640321"]["prp"]["1000"]
     with m2.Engine(115640321, "prp") as e, m2.Gec(e, 100) as g:
         assert e.info().path == m2.PATH_LARGE and e.info().n == 1 << 22

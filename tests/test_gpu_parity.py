@@ -157,12 +157,12 @@ def test_gf61_only_refuses_large_transforms(m2):
         m2.Engine(2976221, 1, fields=m2.FIELDS_GF61)
 
 
-def test_fused_wait_runs_out_and_reports_timeout(m2, oracle_mod):
+@pytest.mark.parametrize("p", [18874367, 115640321])   # cooperative launch; groups by arrival ticket (n = 2^22)
+def test_fused_wait_runs_out_and_reports_timeout(m2, oracle_mod, p):
     """Failure detection without a GPU fault: the fused column kernel's flag
-    wait is made to run out (CTA 0's epoch raised past anything its
+    wait is made to run out (group 0's epoch raised past anything its
     predecessor writes); the launch completes, m2_sync reports M2_ETIMEOUT, and
     after a reload the context computes correct results again."""
-    p = 18874367
     with m2.Engine(p, 1, path=m2.PATH_LARGE) as e:
         assert e.info().fused_cols == 1
         start = e.digits()
