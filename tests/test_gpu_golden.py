@@ -4,7 +4,8 @@ config 1: p = 9941 (n = 256), PRP and LL, full residue every 1000 iterations.
 config 2: p = 132049 (n = 4096) full runs, res64 every 1000; 20 seeded primes in
           [159763, 319483] (n = 8192), 10000 iterations, res64 every 1000.
 config 3: p = 57885161 (n = 2^21) and a seeded prime in [73400329, 142606333]
-          (n = 2^22): res64 at the golden checkpoints (1000 / 10000 / 20000).
+          (n = 2^22): PRP res64 at the golden checkpoints (1000 / 10000 / 20000 /
+          21000) and LL res64 at 1000.
 config 4: the 4096 seeded batch exponents (n = 8 ... 4096) through the batched
           engine, res64 after min(p, 2000) squarings, and batched == plain.
 """
