@@ -121,11 +121,12 @@ def test_gec_gf61_fields(m2):
         assert r == ref.res64()
 
 
-def test_gec_refuses_ll_and_zero_block(m2):
-    with m2.Engine(9941, "ll") as e:
-        with pytest.raises(m2.M2Error) as ei:
-            m2.Gec(e, 10)
-        assert ei.value.code == -6
+def test_gec_refuses_ll_prp3_and_zero_block(m2):
+    for mode in ("ll", "prp3"):   # no x_(k+B) = x_k^(2^B) relation
+        with m2.Engine(9941, mode) as e:
+            with pytest.raises(m2.M2Error) as ei:
+                m2.Gec(e, 10)
+            assert ei.value.code == -6
     with m2.Engine(9941, "prp") as e:
         with pytest.raises(m2.M2Error) as ei:
             m2.Gec(e, 0)

@@ -73,7 +73,7 @@ def test_large_path_vs_oracle(m2, oracle_mod, p, mode):
 
 
 @pytest.mark.parametrize("p", [18874367, 36700159, 57885161, 115640321])   # row pass of 1024 / 2048, 1024-row columns
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 def test_large_path_long_rows_vs_oracle(m2, oracle_mod, p, mode):
     iters = 2
     with m2.Engine(p, mode, path=m2.PATH_LARGE) as e:
