@@ -40,8 +40,9 @@ enum { M2_PATH_AUTO = 0, M2_PATH_SMALL = 1, M2_PATH_LARGE = 2 };
  * reference engine, default), or GF(P61^2) alone with the GF61 prototype's
  * size rule ln + 2((p >> ln) + 1) < 61
  * (gf61_ntt_prp_opencl_inplace_nobitrev_fused.cpp:124-132): up to twice the
- * digits, of up to half the width.  GF(P61^2)-only runs on the one-CTA path (n <= 16384,
- * p < 376832); results are the same residues, in that layout's digits. */
+ * digits, of up to half the width.  Every word of the convolution is then the
+ * signed GF(P61) residue, with no CRT; results are the same residues, in that
+ * layout's digits.  Both paths and every transform size serve it. */
 enum { M2_FIELDS_DUAL = 0, M2_FIELDS_GF61 = 1 };
 
 enum {

@@ -348,7 +348,7 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
     if (opts) o = *opts;
     if (o.fields != M2_FIELDS_DUAL && o.fields != M2_FIELDS_GF61) return M2_EINVAL;
     const bool gf61 = (o.fields == M2_FIELDS_GF61);
-    if (m2::transform_log2(p, gf61 ? 61 : 92) > (gf61 ? 14 : 30)) return M2_EUNSUPPORTED;
+    if (m2::transform_log2(p, gf61 ? 61 : 92) > 30) return M2_EUNSUPPORTED;
     std::unique_ptr<m2_ctx> c(new (std::nothrow) m2_ctx());
     if (!c) return M2_ENOMEM;
     c->L = m2::make_layout(p, gf61 ? 61 : 92);
@@ -363,8 +363,7 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
     int path = o.path;
     // a lone test of h >= 2048 runs faster on the three-pass path's many CTAs
     // than in one CTA (the one-CTA path pays off when many tests share a launch)
-    if (path == M2_PATH_AUTO) path = (h <= 1024 || gf61) ? M2_PATH_SMALL : M2_PATH_LARGE;
-    if (gf61 && path != M2_PATH_SMALL) return M2_EUNSUPPORTED;   // the one-CTA kernel only
+    if (path == M2_PATH_AUTO) path = (h <= 1024) ? M2_PATH_SMALL : M2_PATH_LARGE;
     if (path == M2_PATH_SMALL && h > 8192) return M2_EUNSUPPORTED;
     if (path == M2_PATH_LARGE && !plan_large(c->L, c->span, o.carry_pairs, c->plan)) return M2_EUNSUPPORTED;
     c->path = path;
@@ -405,6 +404,7 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
     } else {
         const m2k::LargePlan& P = raw->plan;
         raw->plan.mode = mode;
+        raw->plan.gf61 = gf61 ? 1u : 0u;
         if ((rc = dalloc(raw, &raw->d_carries, sizeof(i64) * (size_t)P.R * P.G)) ||
             (rc = dalloc(raw, &raw->d_za, sizeof(ulonglong2) * h)) || (rc = dalloc(raw, &raw->d_zb, sizeof(uint2) * h)) ||
             (rc = dalloc(raw, &raw->d_flags, flags_bytes(P)))) {

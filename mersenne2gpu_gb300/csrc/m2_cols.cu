@@ -93,16 +93,23 @@ __device__ __forceinline__ u32 unrot31f(u32 s, u32 ln1) { u32 t = s + ln1; t = t
 // t = mul z + c + 2^(w-1), digit = (t mod 2^w) - 2^(w-1), carry out t >> w.
 // The carry out is below 2^62 in magnitude for every exponent of the table,
 // so it is formed from the 128-bit t by a 64-bit funnel shift.  1 <= w <= 63.
-__device__ __forceinline__ i64 crt_digit(u64 r61, u32 r31, u32 w, u32 mul, i64 sub, i64& c, u32& bad) {
+__device__ __forceinline__ i64 crt_digit(u64 r61, u32 r31, u32 w, u32 mul, i64 sub, i64& c, u32& bad, bool gf61) {
     // canonical residues
     r61 = (r61 == P61) ? 0 : r61;
+    u64 lo, hi;
+    if (gf61) {
+        // GF(P61^2)-only layout: the word is the residue in (-P61/2, P61/2]
+        const bool neg = r61 > (P61 >> 1);
+        lo = neg ? r61 - P61 : r61;
+        hi = neg ? ~0ull : 0ull;
+    } else {
     r31 = (r31 == P31) ? 0 : r31;
     u64 u = r61 + (P61 - r31);                     // (r61 - r31) mod P61, < 2 P61
     u = (u >= P61) ? u - P61 : u;
     u += ((u << 31) & P61) | (u >> 30);            // + u 2^31 (a 61-bit rotation)
     u = (u >= P61) ? u - P61 : u;                  // u = (r61 - r31) (2^31 + 1) mod P61
     // L = u P31 + r31 = u 2^31 - u + r31 < P61 P31
-    u64 lo = u << 31, hi = u >> 33;
+    lo = u << 31; hi = u >> 33;
     const u64 lo2 = lo - u;
     hi -= (lo2 > lo);
     lo = lo2 + r31;
@@ -114,6 +121,7 @@ __device__ __forceinline__ i64 crt_digit(u64 r61, u32 r31, u32 w, u32 mul, i64 s
         const u64 l2 = lo - MLO;
         hi = hi - MHI - (l2 > lo);
         lo = l2;
+    }
     }
     // t = mul z + c + half  (two's complement in hi:lo)
     if (mul == 3) {
@@ -342,8 +350,8 @@ __device__ __forceinline__ void inv_row_stage(const S6c& z, const LargePlan& P, 
                 const u64 j = j0 + 2 * cc;
                 const u64 bp1 = bitpos(p, ln, j + 1), bp2 = bitpos(p, ln, j + 2);
                 const i64 sub = (P.mode == LL && j == 0) ? 2 : 0;
-                d[2 * cc] = crt_digit(x0, y0, (u32)(bp1 - bp), mul, sub, c, bad);
-                d[2 * cc + 1] = crt_digit(x1, y1, (u32)(bp2 - bp1), mul, 0, c, bad);
+                d[2 * cc] = crt_digit(x0, y0, (u32)(bp1 - bp), mul, sub, c, bad, P.gf61 != 0);
+                d[2 * cc + 1] = crt_digit(x1, y1, (u32)(bp2 - bp1), mul, 0, c, bad, P.gf61 != 0);
                 bp = bp2;
             }
         }

@@ -512,7 +512,7 @@ __global__ void __launch_bounds__(LTC, 2) k_cols_inv(LargePlan P, LargeBufs bf) 
         for (int cc = 0; cc < C; ++cc) {
             const u64 e = e0 + cc, j = 2 * e;
             i128 z0, z1;
-            unweigh_crt(z.ld(t * C + cc), j, bf.w61, bf.w31, ln, P.mode, 0, z0, z1);
+            unweigh_crt(z.ld(t * C + cc), j, bf.w61, bf.w31, ln, P.mode, (int)P.gf61, z0, z1);
             if (P.mode == LL && e == 0) z0 -= 2;
             const i64 d0 = split_balanced(z0 + c, width_of(p, ln, j), c);
             const i64 d1 = split_balanced(z1 + c, width_of(p, ln, j + 1), c);

@@ -38,6 +38,7 @@ struct LargePlan {
     unsigned int p;
     int mode;
     unsigned int mid_tickets;  // fused column kernel: 0 = cooperative (CTA index = group), 1 = groups by arrival ticket
+    unsigned int gf61;         // 1: the GF(P61^2)-only layout; each word is the signed GF(P61) residue (no CRT)
 };
 
 struct LargeBufs {

@@ -152,9 +152,31 @@ def test_gf61_only_matches_dual_fields(m2, p, mode):
             assert a.res64() == b.res64(), p
 
 
-def test_gf61_only_refuses_large_transforms(m2):
-    with pytest.raises(m2.M2Error, match=r"\(-6\)"):
-        m2.Engine(2976221, 1, fields=m2.FIELDS_GF61)
+@pytest.mark.parametrize("p,n", [(2976221, 1 << 18), (18874367, 1 << 20)])
+def test_gf61_only_three_pass_matches_dual_fields(m2, p, n):
+    """GF(P61^2)-only layouts on the three-pass path: the generic kernels
+    (n = 2^18: 256 x 512) and the quad-shuffle ones with the cooperative fused
+    column pass (n = 2^20: 256 x 2048) give the dual-field engine's residues."""
+    with m2.Engine(p, 1, fields=m2.FIELDS_GF61) as a, m2.Engine(p, 1) as b:
+        assert a.info().path == m2.PATH_LARGE and a.info().n == n and b.info().n == n // 2
+        for _ in range(2):
+            a.iterate(500)
+            b.iterate(500)
+            assert a.res64() == b.res64(), p
+
+
+def test_gf61_only_n2_22_against_gmp(m2):
+    """p = 57885161 in the GF(P61^2)-only layout (n = 2^22, the fused column pass
+    by arrival ticket): PRP and LL residues at 1000 equal GMP's."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "large.json")) as f:
+        g = json.load(f)["57885161"]
+    for mode, name in ((1, "prp"), (0, "ll")):
+        with m2.Engine(57885161, mode, fields=m2.FIELDS_GF61) as e:
+            assert e.info().n == 1 << 22 and e.info().fused_cols == 1
+            e.iterate(1000)
+            assert f"{e.res64():016x}" == g[name]["1000"], name
 
 
 @pytest.mark.parametrize("p", [18874367, 115640321])   # cooperative launch; groups by arrival ticket (n = 2^22)
