@@ -350,12 +350,18 @@ def run_gec(a, stream) -> dict:
 
 
 # ---------------------------------------------------------------- batched
-def run_batched(count: int, plain_sample: int) -> dict:
+def run_batched(count: int, plain_sample: int, mul_peak: float | None = None) -> dict:
     import mersenne2gpu_gb300 as m2
     from mersenne2gpu_gb300.workloads import batch_exponents
     ps = batch_exponents(count)
     br = m2.batch_run(ps)
     tests_per_s = count / br.seconds if br.seconds > 0 else None
+    # integer-multiply roofline of the batch: sum over tests of p squarings x W(h)
+    wide = sum(p * wide_mul_count(m2.layout(p)[1] // 2) for p in ps)
+    roof = None
+    if mul_peak and br.seconds > 0:
+        roof = {"wide_muls": wide, "peak_products_per_s": mul_peak, "t_mul_s": wide / mul_peak,
+                "achieved_products_per_s": wide / br.seconds, "frac": (wide / mul_peak) / br.seconds}
     # plain path: one test at a time, a stratified sample over the sorted exponents
     order = sorted(range(count), key=lambda i: ps[i])
     pick = [order[int((k + 0.5) * count / plain_sample)] for k in range(plain_sample)]
@@ -379,7 +385,7 @@ def run_batched(count: int, plain_sample: int) -> dict:
         "plain_sample": f"{plain_sample} tests one at a time (stratified by p), mean time extrapolated",
         "speedup_vs_plain": (tests_per_s / plain_tests_per_s) if (tests_per_s and plain_tests_per_s) else None,
         "bit_exact_vs_plain": f"{same}/{plain_sample}", "buckets": br.buckets, "launches": br.launches,
-        "primes_found": int(br.is_prime.sum()),
+        "primes_found": int(br.is_prime.sum()), "roofline_imad": roof,
         "tuned_threads_per_bucket": {f"n=2^{ln}": {"threads": t[0], "ns_per_test_squaring": round(t[1], 1)}
                                      for ln in range(3, 14) if (t := m2.batch_tuned(ln)) is not None},
     }
@@ -537,7 +543,7 @@ def run_gb300(a, dist: Dist) -> dict | None:
             out["gerbicz"] = {"error": str(ex)}
     if a.batch:
         try:
-            out["batched"] = run_batched(a.batch_count, a.plain_sample)
+            out["batched"] = run_batched(a.batch_count, a.plain_sample, mul_peak)
         except Exception as ex:  # noqa: BLE001
             out["batched"] = {"error": str(ex)}
     if a.serve:
