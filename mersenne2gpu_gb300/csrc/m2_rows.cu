@@ -110,8 +110,13 @@ __device__ __forceinline__ void gstore(const LargeBufs& bf, u64 e, const E& v) {
 // (block JB0 + l, or JB0 + 3 - l when mirrored, at 4 SA_ blocks) and stores
 // k = 4l + m (store(m, v)).  The inverse loads k = 4l + m, runs the same steps
 // backwards and stores k = l + 4m.
-template <class LOAD, class STORE>
-__device__ __forceinline__ void pass16_fwd(LOAD&& load, STORE&& store, u32 l, const DTw* tw4, u64 SA_, u64 JA, u64 JB0, bool mir) {
+// The quad's exchange between the two levels goes through the sub-column's
+// own shared-memory slots: the first level's outputs are stored where k = l + 4m
+// lies (xst(m, v)), and after a warp barrier each lane reads k = 4l + m
+// (xld(m)).  No other quad touches those 16 slots during the pass.
+template <class LOAD, class STORE, class XST, class XLD>
+__device__ __forceinline__ void pass16_fwd(LOAD&& load, STORE&& store, XST&& xst, XLD&& xld, u32 l, const DTw* tw4, u64 SA_,
+                                           u64 JA, u64 JB0, bool mir) {
     E x[4];
 #pragma unroll
     for (int m = 0; m < 4; ++m) x[m] = load(m);
@@ -119,7 +124,11 @@ __device__ __forceinline__ void pass16_fwd(LOAD&& load, STORE&& store, u32 l, co
         const Tri A = tri(tw4, SA_, JA, mir);
         dif4(x[0], x[1], x[2], x[3], A.r1, A.r2, A.r3);
     }
-    quad_transpose(x, l);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) xst(m, x[m]);
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < 4; ++m) x[m] = xld(m);
     {
         const Tri Bt = tri(tw4, 4 * SA_, JB0 + (mir ? 3 - l : l), mir);
         dif4(x[0], x[1], x[2], x[3], Bt.r1, Bt.r2, Bt.r3);
@@ -127,8 +136,11 @@ __device__ __forceinline__ void pass16_fwd(LOAD&& load, STORE&& store, u32 l, co
 #pragma unroll
     for (int m = 0; m < 4; ++m) store(m, x[m]);
 }
-template <class LOAD, class STORE>
-__device__ __forceinline__ void pass16_inv(LOAD&& load, STORE&& store, u32 l, const DTw* tw4, u64 SA_, u64 JA, u64 JB0, bool mir) {
+// the inverse: loads k = 4l + m, exchanges through xst (k = 4l + m) and xld
+// (k = l + 4m), stores k = l + 4m
+template <class LOAD, class STORE, class XST, class XLD>
+__device__ __forceinline__ void pass16_inv(LOAD&& load, STORE&& store, XST&& xst, XLD&& xld, u32 l, const DTw* tw4, u64 SA_,
+                                           u64 JA, u64 JB0, bool mir) {
     E x[4];
 #pragma unroll
     for (int m = 0; m < 4; ++m) x[m] = load(m);
@@ -136,7 +148,11 @@ __device__ __forceinline__ void pass16_inv(LOAD&& load, STORE&& store, u32 l, co
         const Tri Bt = tri(tw4, 4 * SA_, JB0 + (mir ? 3 - l : l), mir);
         dit4(x[0], x[1], x[2], x[3], Bt.r1, Bt.r2, Bt.r3);
     }
-    quad_transpose(x, l);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) xst(m, x[m]);
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < 4; ++m) x[m] = xld(m);
     {
         const Tri A = tri(tw4, SA_, JA, mir);
         dit4(x[0], x[1], x[2], x[3], A.r1, A.r2, A.r3);
@@ -185,9 +201,11 @@ __global__ void __launch_bounds__(512, 2) k_rows_q(LargePlan P, LargeBufs bf) {
         const u32 trow = sl ? t1 : t0;
         const bool mir = general && sl;
         const u32 tsrc = mir ? t0 : trow;
-        const u32 ps = swz(sl * B + i) ^ swz(SA * 4 * l);                    // stores k = 4l + m
+        const u32 pb = swz(sl * B + i), ps = pb ^ swz(SA * 4 * l), pk = pb ^ swz(SA * l);   // k = 4l + m; k = l + 4m
         pass16_fwd([&](int m) { return gload(bf, (u64)trow * B + i + (u64)SA * (l + 4 * m)); },
-                   [&](int m, const E& v) { z.stp(ps ^ swz(SA * m), v); }, l, bf.tw4, R, tsrc, 4ull * tsrc, mir);
+                   [&](int m, const E& v) { z.stp(ps ^ swz(SA * m), v); },
+                   [&](int m, const E& v) { z.stp(pk ^ swz(SA * 4 * m), v); }, [&](int m) { return z.ldp(ps ^ swz(SA * m)); },
+                   l, bf.tw4, R, tsrc, 4ull * tsrc, mir);
     }
     __syncthreads();
     // ---------------- pass B: levels 3-4 ----------------
@@ -201,6 +219,7 @@ __global__ void __launch_bounds__(512, 2) k_rows_q(LargePlan P, LargeBufs bf) {
         const u32 base = sl * B + jb * MB + ib;
         const u32 pb = swz(base), pl = pb ^ swz(SB * l), p4l = pb ^ swz(SB * 4 * l);
         pass16_fwd([&](int m) { return z.ldp(pl ^ swz(SB * 4 * m)); }, [&](int m, const E& v) { z.stp(p4l ^ swz(SB * m), v); },
+                   [&](int m, const E& v) { z.stp(pl ^ swz(SB * 4 * m), v); }, [&](int m) { return z.ldp(p4l ^ swz(SB * m)); },
                    l, bf.tw4, 16 * R, 16ull * tsrc + jj, 64ull * tsrc + 4 * jj, mir);
     }
     __syncthreads();
@@ -322,6 +341,7 @@ __global__ void __launch_bounds__(512, 2) k_rows_q(LargePlan P, LargeBufs bf) {
         const u32 base = sl * B + jb * MB + ib;
         const u32 pb = swz(base), pl = pb ^ swz(SB * l), p4l = pb ^ swz(SB * 4 * l);
         pass16_inv([&](int m) { return z.ldp(p4l ^ swz(SB * m)); }, [&](int m, const E& v) { z.stp(pl ^ swz(SB * 4 * m), v); },
+                   [&](int m, const E& v) { z.stp(p4l ^ swz(SB * m), v); }, [&](int m) { return z.ldp(pl ^ swz(SB * 4 * m)); },
                    l, bf.tw4, 16 * R, 16ull * tsrc + jj, 64ull * tsrc + 4 * jj, mir);
     }
     __syncthreads();
@@ -333,10 +353,11 @@ __global__ void __launch_bounds__(512, 2) k_rows_q(LargePlan P, LargeBufs bf) {
         const u32 trow = sl ? t1 : t0;
         const bool mir = general && sl;
         const u32 tsrc = mir ? t0 : trow;
-        const u32 pl = swz(sl * B + i) ^ swz(SA * 4 * l);                    // loads k = 4l + m
+        const u32 pb = swz(sl * B + i), pl = pb ^ swz(SA * 4 * l), pk = pb ^ swz(SA * l);   // k = 4l + m; k = l + 4m
         pass16_inv([&](int m) { return z.ldp(pl ^ swz(SA * m)); },
-                   [&](int m, const E& v) { gstore(bf, (u64)trow * B + i + (u64)SA * (l + 4 * m), v); }, l, bf.tw4, R, tsrc,
-                   4ull * tsrc, mir);
+                   [&](int m, const E& v) { gstore(bf, (u64)trow * B + i + (u64)SA * (l + 4 * m), v); },
+                   [&](int m, const E& v) { z.stp(pl ^ swz(SA * m), v); }, [&](int m) { return z.ldp(pk ^ swz(SA * 4 * m)); },
+                   l, bf.tw4, R, tsrc, 4ull * tsrc, mir);
     }
 }
 
