@@ -141,7 +141,10 @@ __device__ __forceinline__ i64 crt_digit(u64 r61, u32 r31, u32 w, u32 mul, i64 s
 }
 
 // the 16-element sub-column passes over the columns (rows i + stride k of a
-// block; base < stride, so base and stride k sit on disjoint bits)
+// block; base < stride, so base and stride k sit on disjoint bits).  Lane l of
+// the quad loads k = l + 4m, runs the first level, and hands its outputs on
+// through the same slots: after a warp barrier it reads k = 4l + m, runs the
+// second level and stores there (no other quad touches the 16 slots).
 __device__ __forceinline__ void colpass_fwd(const S6c& z, u32 base, u32 stride, u32 l, const DTw* tw4, u64 SA_, u64 JA, u64 JB0) {
     const u32 pb = swzc(base), pl = pb ^ swzc(stride * l), p4l = pb ^ swzc(stride * 4 * l);
     E x[4];
@@ -149,7 +152,11 @@ __device__ __forceinline__ void colpass_fwd(const S6c& z, u32 base, u32 stride, 
     for (int m = 0; m < 4; ++m) x[m] = z.ldp(pl ^ swzc(stride * 4 * m));
     if (SA_ == 1) dif4_1(x[0], x[1], x[2], x[3]);   // the first level: root 1
     else { const Tri A = tri(tw4, SA_, JA); dif4(x[0], x[1], x[2], x[3], A.r1, A.r2, A.r3); }
-    quad_transpose(x, l);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) z.stp(pl ^ swzc(stride * 4 * m), x[m]);
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < 4; ++m) x[m] = z.ldp(p4l ^ swzc(stride * m));
     { const Tri Bt = tri(tw4, 4 * SA_, JB0 + l); dif4(x[0], x[1], x[2], x[3], Bt.r1, Bt.r2, Bt.r3); }
 #pragma unroll
     for (int m = 0; m < 4; ++m) z.stp(p4l ^ swzc(stride * m), x[m]);
@@ -160,7 +167,11 @@ __device__ __forceinline__ void colpass_inv(const S6c& z, u32 base, u32 stride, 
 #pragma unroll
     for (int m = 0; m < 4; ++m) x[m] = z.ldp(p4l ^ swzc(stride * m));
     { const Tri Bt = tri(tw4, 4 * SA_, JB0 + l); dit4(x[0], x[1], x[2], x[3], Bt.r1, Bt.r2, Bt.r3); }
-    quad_transpose(x, l);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) z.stp(p4l ^ swzc(stride * m), x[m]);
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < 4; ++m) x[m] = z.ldp(pl ^ swzc(stride * 4 * m));
     if (SA_ == 1) dit4_1(x[0], x[1], x[2], x[3]);   // the first level: root 1
     else { const Tri A = tri(tw4, SA_, JA); dit4(x[0], x[1], x[2], x[3], A.r1, A.r2, A.r3); }
 #pragma unroll
