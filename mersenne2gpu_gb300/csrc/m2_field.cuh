@@ -244,21 +244,6 @@ __device__ __forceinline__ E shfl_xor_e(const E& v, int m) {
     r.d = __shfl_xor_sync(0xffffffffu, v.d, m);
     return r;
 }
-// In a quad of lanes, lane l slot m holds M[l][m]; afterwards it holds M[m][l].
-__device__ __forceinline__ void quad_transpose(E (&x)[4], u32 l) {
-    {
-        const bool hi = (l & 2u) != 0;
-        const E s0 = hi ? x[0] : x[2], s1 = hi ? x[1] : x[3];
-        const E r0 = shfl_xor_e(s0, 2), r1 = shfl_xor_e(s1, 2);
-        if (hi) { x[0] = r0; x[1] = r1; } else { x[2] = r0; x[3] = r1; }
-    }
-    {
-        const bool hi = (l & 1u) != 0;
-        const E s0 = hi ? x[0] : x[1], s1 = hi ? x[2] : x[3];
-        const E r0 = shfl_xor_e(s0, 1), r1 = shfl_xor_e(s1, 1);
-        if (hi) { x[0] = r0; x[2] = r1; } else { x[1] = r0; x[3] = r1; }
-    }
-}
 
 // ---------------- digits <-> field ----------------
 __device__ __forceinline__ u64 digit_to61(i64 d) { return d >= 0 ? (u64)d : P61 - (u64)(-d); }
