@@ -169,24 +169,6 @@ template <class T> int dalloc(m2_ctx* c, T** p, size_t bytes) {
 // counter (G is even, so the counter is 8-byte aligned)
 size_t flags_bytes(const m2k::LargePlan& P) { return sizeof(unsigned) * ((size_t)P.G + 2); }
 
-bool plan_large(const m2::Layout& L, int span, u32 carry_pairs, m2k::LargePlan& P) {
-    const int Lh = L.ln - 1;
-    if (Lh < 6) return false;
-    int L1 = 2 * (Lh / 4);
-    if (L1 < 2) L1 = 2;
-    const int L2 = Lh - L1;
-    P.ln = L.ln; P.L = Lh; P.L1 = L1; P.L2 = L2;
-    P.R = 1u << L1; P.B = 1u << L2;
-    P.span = span; P.p = L.p;
-    // columns per CTA: 4 (the quad-shuffle column kernels' shape for R = 256
-    // and 1024, and more CTAs for the small grids of the other mid-size plans)
-    u32 C = 4;
-    if (carry_pairs >= 4 && carry_pairs <= 16 && (carry_pairs & (carry_pairs - 1)) == 0) C = carry_pairs;
-    while (2 * C < (u32)span + 1 && C < 16) C <<= 1;
-    if (2 * C < (u32)span + 1 || C > P.B) return false;
-    P.C = C; P.G = P.B / C;
-    return true;
-}
 
 // Iterations of the three-pass path per graph replay: 3 kernel nodes each.
 constexpr uint32_t GRAPH_ITERS = 50;
@@ -268,6 +250,28 @@ int read_head(m2_ctx* c, std::vector<u64>& head, unsigned& flags) {
 }  // namespace
 
 namespace m2i {
+// Plan of the three-pass path: rows 4^floor(log2 h / 4), row length h / rows,
+// C columns per CTA (carry_pairs when it is a power of two in [4, 16], else 4,
+// widened until a segment of 2C digits exceeds the carry span).
+bool plan_large(const m2::Layout& L, int span, uint32_t carry_pairs, m2k::LargePlan& P) {
+    const int Lh = L.ln - 1;
+    if (Lh < 6) return false;
+    int L1 = 2 * (Lh / 4);
+    if (L1 < 2) L1 = 2;
+    const int L2 = Lh - L1;
+    P.ln = L.ln; P.L = Lh; P.L1 = L1; P.L2 = L2;
+    P.R = 1u << L1; P.B = 1u << L2;
+    P.span = span; P.p = L.p;
+    // columns per CTA: 4 (the quad-shuffle column kernels' shape for R = 256
+    // and 1024, and more CTAs for the small grids of the other mid-size plans)
+    uint32_t C = 4;
+    if (carry_pairs >= 4 && carry_pairs <= 16 && (carry_pairs & (carry_pairs - 1)) == 0) C = carry_pairs;
+    while (2 * C < (uint32_t)span + 1 && C < 16) C <<= 1;
+    if (2 * C < (uint32_t)span + 1 || C > P.B) return false;
+    P.C = C; P.G = P.B / C;
+    return true;
+}
+
 const m2::Layout& layout(const m2_ctx* c) { return c->L; }
 m2_opts creation_opts(const m2_ctx* c) { return c->opts; }
 cudaStream_t stream(const m2_ctx* c) { return c->stream; }
@@ -365,7 +369,7 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
     // than in one CTA (the one-CTA path pays off when many tests share a launch)
     if (path == M2_PATH_AUTO) path = (h <= 1024) ? M2_PATH_SMALL : M2_PATH_LARGE;
     if (path == M2_PATH_SMALL && h > 8192) return M2_EUNSUPPORTED;
-    if (path == M2_PATH_LARGE && !plan_large(c->L, c->span, o.carry_pairs, c->plan)) return M2_EUNSUPPORTED;
+    if (path == M2_PATH_LARGE && !m2i::plan_large(c->L, c->span, o.carry_pairs, c->plan)) return M2_EUNSUPPORTED;
     c->path = path;
     if (o.stream) { c->stream = (cudaStream_t)o.stream; }
     else {

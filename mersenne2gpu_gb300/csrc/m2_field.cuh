@@ -72,21 +72,30 @@ __device__ __forceinline__ u32 rotl31(u32 x, u32 s) {
 }
 
 // ---------------- complex products ----------------
-// (a0 + a1 i)(b0 + b1 i) in GF(P61^2).  The real part a0 b0 - a1 b1 is formed
-// as a0 b0 + a1 (2 P61 - b1): a 64-bit offset of one factor instead of a
-// 128-bit one of the product (2 P61 lies above every coordinate).  With
-// coordinates up to 2^61 + 7 every sum stays below 3 2^122, within red61's
-// bound of 7 2^122.
+// (a0 + a1 i)(b0 + b1 i) in GF(P61^2) with three 64x64->128-bit products
+// (Karatsuba): p0 = a0 b0, p1 = a1 b1, k = (a0 + a1)(b0 + b1); the real part
+// is p0 - p1, taken as p0 + (C - p1) with C = P61 2^62 above every p1, the
+// imaginary part k - p0 - p1 = a0 b1 + a1 b0 is exact.  The integer pipe runs
+// each 128-bit product as four wide multiplies on the multiply-add pipe, the
+// busier of the two; the extra 128-bit additions go to the ALU pipe.  With
+// a in [0, 2^61 + 7] and b in [0, P61] both results stay below 2^124, the bound
+// of red61.
+__device__ __forceinline__ u128 mul128(u64 a, u64 b) { return (u128)a * b; }
+constexpr u128 KM61 = (u128)P61 << 62;
 __device__ __forceinline__ void cmul61(u64 a0, u64 a1, u64 b0, u64 b1, u64& r0, u64& r1) {
-    const u128 re = (u128)a0 * b0 + (u128)a1 * (K2_61 - b1);
-    const u128 im = (u128)a0 * b1 + (u128)a1 * b0;
+    const u128 p0 = mul128(a0, b0), p1 = mul128(a1, b1), k = mul128(a0 + a1, b0 + b1);
+    const u128 re = p0 + (KM61 - p1);
+    const u128 im = k - p0 - p1;
     r0 = red61((u64)re, (u64)(re >> 64));
     r1 = red61((u64)im, (u64)(im >> 64));
 }
-// (a0 + a1 i) * conj(b0 + b1 i)
+// (a0 + a1 i) * conj(b0 + b1 i): the real part p0 + p1; the imaginary part
+// a1 b0 - a0 b1 as (a0 + a1)(b0 + P61 - b1) - p0 + p1, which adds the
+// multiple (a0 + a1) P61 and so is never negative, and stays below 2^124
 __device__ __forceinline__ void cmulconj61(u64 a0, u64 a1, u64 b0, u64 b1, u64& r0, u64& r1) {
-    const u128 re = (u128)a0 * b0 + (u128)a1 * b1;
-    const u128 im = (u128)a1 * b0 + (u128)a0 * (K2_61 - b1);
+    const u128 p0 = mul128(a0, b0), p1 = mul128(a1, b1), k = mul128(a0 + a1, b0 + (P61 - b1));
+    const u128 re = p0 + p1;
+    const u128 im = k - p0 + p1;
     r0 = red61((u64)re, (u64)(re >> 64));
     r1 = red61((u64)im, (u64)(im >> 64));
 }

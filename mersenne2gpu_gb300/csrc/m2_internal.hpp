@@ -7,7 +7,13 @@
 
 #include <cuda_runtime_api.h>
 
+namespace m2k { struct LargePlan; }
+
 namespace m2i {
+
+// plan of the three-pass path for exponent layout L (false: no plan fits);
+// carry_pairs is the -B hint (columns per CTA), 0 for the default
+bool plan_large(const m2::Layout& L, int span, uint32_t carry_pairs, m2k::LargePlan& P);
 
 // digit widths and bit positions of the context's residue
 const m2::Layout& layout(const m2_ctx* c);

@@ -548,7 +548,7 @@ cudaError_t large_setup(const LargePlan& P) {
 
 cudaError_t launch_large_stage(const LargePlan& P, const LargeBufs& b, int stage, cudaStream_t s) {
     const size_t sc = large_smem_cols(P), sr = large_smem_rows(P);
-    if (stage == STAGE_MID) return launch_cols_mid(P, b, s);
+    if (stage == STAGE_MID) return b.flags ? launch_cols_mid(P, b, s) : cudaErrorInvalidValue;
     if (stage != 1 && cols_q_supported(P)) return launch_cols_q(P, b, stage == 2, s);
     if (stage == 0) {
 #define M2_FWD(CC) if (P.C == CC) k_cols_fwd<CC><<<P.G, LTC, sc, s>>>(P, b);

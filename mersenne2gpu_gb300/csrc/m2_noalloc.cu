@@ -24,6 +24,7 @@
 #include "../../include/m2gpu.h"
 #include "m2_field.cuh"
 #include "m2_host.hpp"
+#include "m2_internal.hpp"
 #include "m2_kernels.cuh"
 
 #include <cuda_runtime.h>
@@ -51,21 +52,6 @@ void* g_addr[kMaxDevices] = {};
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// Same plan rule as the three-pass path of m2_create (rows = 4^floor(log2 h / 4)).
-bool make_plan(const m2::Layout& L, int span, m2k::LargePlan& P) {
-    const int Lh = L.ln - 1;
-    int L1 = 2 * (Lh / 4);
-    if (L1 < 2) L1 = 2;
-    P.ln = L.ln; P.L = Lh; P.L1 = L1; P.L2 = Lh - L1;
-    P.R = 1u << L1; P.B = 1u << P.L2;
-    P.span = span; P.p = L.p;
-    unsigned C = 16;
-    while (C > 4 && 24ull * C * P.R > 100 * 1024) C >>= 1;
-    while (2 * C < (unsigned)span + 1 && C < 16) C <<= 1;
-    if (2 * C < (unsigned)span + 1 || C > P.B) return false;
-    P.C = C; P.G = P.B / C;
-    return true;
-}
 
 __device__ __forceinline__ E dpow(E x, unsigned long long e) {
     E r{1, 0, 1, 0};
@@ -112,18 +98,25 @@ __device__ __forceinline__ unsigned width_at(unsigned p, int ln, unsigned long l
     return (unsigned)(bitpos_of(p, ln, j + 1) - bitpos_of(p, ln, j));
 }
 
-// Caller digits in [0, 2^w) (or any |d| < 2^w) -> digits within 2^(w-1) + 1 of
-// zero, same residue: each digit sheds 2^w when it is >= 2^(w-1) and hands 1 to
-// the next digit (the top digit's 1 goes to digit 0, since 2^p == 1 mod M_p).
+// Caller digits with |d| < 2^w -> digits within 2^(w-1) + 1 of zero, same
+// residue: a digit at or above 2^(w-1) sheds 2^w and hands +1 to the next
+// digit, a digit below -2^(w-1) gains 2^w and hands -1 on (the top digit's
+// unit goes to digit 0, since 2^p == 1 mod M_p).  Each digit keeps a value in
+// [-2^(w-1), 2^(w-1)) and receives at most one unit, so every accepted input
+// starts the first squaring inside the headroom the transform size assumes.
+__device__ __forceinline__ long long shed(long long x, unsigned w, long long& unit) {
+    if (w == 0) { unit = 0; return x; }
+    const long long half = 1ll << (w - 1);
+    unit = (x >= half) ? 1 : (x < -half ? -1 : 0);
+    return x - (unit << w);
+}
 __global__ void k_noalloc_rebalance(long long* d, const long long* src_copy, unsigned n, unsigned p, int ln) {
     for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const unsigned w = width_at(p, ln, j);
         const unsigned jm = (j + n - 1) % n;
-        const unsigned wm = width_at(p, ln, jm);
-        const long long x = src_copy[j], xm = src_copy[jm];
-        const long long out = (w && x >= (1ll << (w - 1))) ? x - (1ll << w) : x;
-        const long long in = (wm && xm >= (1ll << (wm - 1))) ? 1 : 0;
-        d[j] = out + in;
+        long long unit_out, unit_in;
+        const long long out = shed(src_copy[j], width_at(p, ln, j), unit_out);
+        shed(src_copy[jm], width_at(p, ln, jm), unit_in);
+        d[j] = out + unit_in;
     }
 }
 __global__ void k_noalloc_copy(long long* dst, const long long* src, unsigned n) {
@@ -174,8 +167,11 @@ extern "C" int m2_square_noalloc(uint32_t p, int mode, int64_t* digits, uint32_t
     m2::Layout L;
     L.p = p; L.ln = ln; L.n = 1ull << ln; L.h = L.n / 2; L.q = p >> ln;
     const int span = m2::carry_span(L);
+    // the plan of m2_create's three-pass path; at these sizes (n <= 2^18, rows
+    // of at most 512) it runs the generic column and row kernels, never the
+    // fused column pass, whose epoch flags and ticket this path does not carry
     m2k::LargePlan P{};
-    if (!make_plan(L, span, P)) return M2_EUNSUPPORTED;
+    if (!m2i::plan_large(L, span, 0, P)) return M2_EUNSUPPORTED;
     P.mode = mode;
     const unsigned h = (unsigned)L.h, n = (unsigned)L.n;
     unsigned smax = 0;
@@ -212,6 +208,9 @@ extern "C" int m2_square_noalloc(uint32_t p, int mode, int64_t* digits, uint32_t
     if (cudaGetLastError() != cudaSuccess) return M2_ECUDA;
 
     if (m2k::large_setup(P) != cudaSuccess) return M2_ECUDA;
+    // flags and ticket stay null: launch_large_iteration runs the separate
+    // column passes only, and launch_large_stage refuses the fused one
+    // (cudaErrorInvalidValue) when a plan's buffers carry no flags
     const m2k::LargeBufs bufs{reinterpret_cast<long long*>(digits), car, za, zb, w61, w31, tw4, tc, status};
     for (uint32_t i = 0; i < iters; ++i)
         if (m2k::launch_large_iteration(P, bufs, st) != cudaSuccess) return M2_ECUDA;

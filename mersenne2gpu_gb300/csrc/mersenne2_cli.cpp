@@ -118,10 +118,10 @@ int main(int argc, char* argv[]) {
     int mode = M2_MODE_LL;
     uint32_t report_every = 1000u;
     double report_seconds = 2.0;
-    uint32_t device_index = 0u, wg_override = 0u, carry_wg_override = 0u, carry_pairs_override = 0u;
-    uint32_t local_stage_cap_override = 0u, max_iters_override = 0u;
-    bool show_defaults_only = false, report_every_set = false, debug_plan = false, want_res64 = false;
-    uint32_t debug_cppint_every = 0u, debug_cppint_max_iter = 0u;
+    uint32_t device_index = 0u, opt_wg = 0u, opt_carry_wg = 0u, opt_carry_pairs = 0u;
+    uint32_t opt_stage_cap = 0u, opt_iter_cap = 0u;
+    bool print_defaults = false, have_report_arg = false, debug_plan = false, want_res64 = false;
+    uint32_t exact_check_every = 0u, exact_check_until = 0u;
     int path = M2_PATH_AUTO;
     int fields = M2_FIELDS_DUAL;
     std::string checkpoint, resume;
@@ -142,25 +142,25 @@ int main(int argc, char* argv[]) {
         } else if (arg == "-R") {
             report_seconds = std::max(0.0, std::atof(need(i, "seconds after -R")));
         } else if (arg == "-W") {
-            wg_override = (uint32_t)std::strtoul(need(i, "work-group size after -W"), nullptr, 10);
+            opt_wg = (uint32_t)std::strtoul(need(i, "work-group size after -W"), nullptr, 10);
         } else if (arg == "-CW") {
-            carry_wg_override = (uint32_t)std::strtoul(need(i, "carry work-group size after -CW"), nullptr, 10);
+            opt_carry_wg = (uint32_t)std::strtoul(need(i, "carry work-group size after -CW"), nullptr, 10);
         } else if (arg == "-B") {
-            carry_pairs_override = (uint32_t)std::strtoul(need(i, "carry_pairs after -B"), nullptr, 10);
+            opt_carry_pairs = (uint32_t)std::strtoul(need(i, "carry_pairs after -B"), nullptr, 10);
         } else if (arg == "-LS") {
-            local_stage_cap_override = (uint32_t)std::strtoul(need(i, "local stage cap after -LS"), nullptr, 10);
+            opt_stage_cap = (uint32_t)std::strtoul(need(i, "local stage cap after -LS"), nullptr, 10);
         } else if (arg == "-N") {
-            max_iters_override = (uint32_t)std::strtoul(need(i, "max iterations after -N"), nullptr, 10);
+            opt_iter_cap = (uint32_t)std::strtoul(need(i, "max iterations after -N"), nullptr, 10);
         } else if (arg == "--show-defaults") {
-            show_defaults_only = true;
+            print_defaults = true;
         } else if (arg == "--debug-plan") {
             debug_plan = true;
         } else if (arg == "--debug-stage-selftest" || arg == "--enable-chunk64") {
             // the reference's optional fused-kernel self-tests; this engine has one kernel set
         } else if (arg == "--debug-cppint-every") {
-            debug_cppint_every = (uint32_t)std::strtoul(need(i, "value after --debug-cppint-every"), nullptr, 10);
+            exact_check_every = (uint32_t)std::strtoul(need(i, "value after --debug-cppint-every"), nullptr, 10);
         } else if (arg == "--debug-cppint-max-iter") {
-            debug_cppint_max_iter = (uint32_t)std::strtoul(need(i, "value after --debug-cppint-max-iter"), nullptr, 10);
+            exact_check_until = (uint32_t)std::strtoul(need(i, "value after --debug-cppint-max-iter"), nullptr, 10);
         } else if (arg == "--res64") {
             want_res64 = true;
         } else if (arg == "--gf61") {
@@ -177,16 +177,16 @@ int main(int argc, char* argv[]) {
             if (gec_block == 0u) { std::cerr << "--gerbicz needs a block length >= 1\n"; return 1; }
         } else if (arg == "--debug-gec-corrupt") {
             corrupt_at = (uint32_t)std::strtoul(need(i, "iteration after --debug-gec-corrupt"), nullptr, 10);
-        } else if (!report_every_set) {
+        } else if (!have_report_arg) {
             report_every = (uint32_t)std::strtoul(arg.c_str(), nullptr, 10);
-            report_every_set = true;
+            have_report_arg = true;
         } else {
             std::cerr << "Unknown argument: " << arg << "\n";
             usage(argv[0]);
             return 1;
         }
     }
-    if (debug_cppint_every != 0u || debug_cppint_max_iter != 0u) {
+    if (exact_check_every != 0u || exact_check_until != 0u) {
         // the reference's exact big-integer check needs Boost (mersenne2_gpu.cpp:3718-3725);
         // this build checks exactness in its test suite instead
         std::cout << "debug_cppint_backend=none\n";
@@ -211,27 +211,27 @@ int main(int argc, char* argv[]) {
     cudaDeviceProp prop{};
     cudaGetDeviceProperties(&prop, (int)device_index);
     std::cout << "device=" << device_index << " (" << prop.name << ")\n";
-    if (!report_every_set) {
+    if (!have_report_arg) {
         // the reference's NVIDIA defaults (mersenne2_gpu.cpp:3779-3788)
         if (h >= (1u << 20)) report_every = 4000u;
         else if (h >= (1u << 18)) report_every = 2000u;
         else report_every = 1000u;
     }
-    const uint32_t wg = wg_override ? wg_override : 256u;
-    const uint32_t carry_wg = carry_wg_override ? carry_wg_override : wg;
-    if (show_defaults_only) {
+    const uint32_t wg = opt_wg ? opt_wg : 256u;
+    const uint32_t carry_wg = opt_carry_wg ? opt_carry_wg : wg;
+    if (print_defaults) {
         std::cout << "vendor=NVIDIA Corporation, compute_units=" << prop.multiProcessorCount << ", max_wg="
                   << prop.maxThreadsPerBlock << ", local_mem=" << prop.sharedMemPerBlockOptin << "\n"
                   << "auto_wg=256, auto_carry_wg=256, auto_carry_pairs=auto, auto_profile=gb300\n"
                   << "effective_wg=" << wg << ", effective_carry_wg=" << carry_wg << ", effective_local_stage_cap="
-                  << (local_stage_cap_override ? local_stage_cap_override : 0u) << ", effective_max_iters=" << max_iters_override << "\n";
+                  << (opt_stage_cap ? opt_stage_cap : 0u) << ", effective_max_iters=" << opt_iter_cap << "\n";
         return 0;
     }
 
     m2_opts o{};
     o.device = (int)device_index;
-    o.wg = wg_override;
-    o.carry_pairs = carry_pairs_override;
+    o.wg = opt_wg;
+    o.carry_pairs = opt_carry_pairs;
     o.path = path;
     o.fields = fields;
     m2_ctx* ctx = nullptr;
@@ -244,7 +244,7 @@ int main(int argc, char* argv[]) {
               << (double)h / (double)blocks << ", carry_target_pairs=" << (large ? info.cols_per_cta : (uint32_t)h)
               << ", tuned_wg=" << wg << ", carry_wg=" << carry_wg << ", local_stage_cap=" << info.row_len
               << ", auto_profile=" << (large ? "gb300-three-pass" : "gb300-one-cta");
-    if (wg_override != 0u || carry_pairs_override != 0u) std::cout << " (manual override)";
+    if (opt_wg != 0u || opt_carry_pairs != 0u) std::cout << " (manual override)";
     std::cout << "\n";
     std::cout.unsetf(std::ios::fixed);
     if (debug_plan) {
@@ -268,7 +268,7 @@ int main(int argc, char* argv[]) {
     }
 
     uint32_t total_iters = info.total_iters;
-    if (max_iters_override != 0u) total_iters = std::min(total_iters, max_iters_override);
+    if (opt_iter_cap != 0u) total_iters = std::min(total_iters, opt_iter_cap);
     uint32_t iter = 0;
     if (!resume.empty()) {
         std::vector<uint64_t> d;
@@ -320,7 +320,7 @@ int main(int argc, char* argv[]) {
         }
         return 0;
     };
-    if (max_iters_override != 0u) std::cout << "benchmark_iters=" << total_iters << "\n";
+    if (opt_iter_cap != 0u) std::cout << "benchmark_iters=" << total_iters << "\n";
     uint32_t batch = std::max<uint32_t>(1u, report_every != 0u ? report_every : 1000u);
     if ((rc = report(iter))) return finish(fail(rc, "report"));
     std::signal(SIGINT, on_sigint);

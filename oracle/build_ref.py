@@ -11,6 +11,8 @@
    only the compile step runs.
 
 Usage: python oracle/build_ref.py [--reference DIR]
+The reference checkout is DIR, else $M2_REFERENCE, else a directory named
+"reference" beside this repository.
 """
 from __future__ import annotations
 
@@ -22,7 +24,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 BUILD_DIR = os.path.join(HERE, "_build")
-DEFAULT_REFERENCE = "/root/reference"
+DEFAULT_REFERENCE = os.environ.get("M2_REFERENCE") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 
 def extract(reference: str) -> bool:

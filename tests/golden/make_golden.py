@@ -28,7 +28,9 @@ sys.path.insert(0, ROOT)
 
 SMALL_P = [3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 61, 89, 107, 127, 521, 607, 1279, 2203, 2281, 3217, 4253, 4423,
            9689, 9941, 11213, 19937, 21701, 23209, 44497, 8191, 8209, 10007, 30011]
-LARGE = {57885161: [1000, 10000, 20000, 21000], 115640321: [1000, 10000, 20000, 21000]}
+# p = 57885161: every 1000 squarings up to 30000, so that a bench run of up to 30
+# report batches of 1000 ends on a checkpoint whatever its warm-up/timed split
+LARGE = {57885161: list(range(1000, 30001, 1000)), 115640321: [1000, 10000, 20000, 21000]}
 LARGE_LL = {57885161: [1000], 115640321: [1000]}   # the LL -2 step through the n = 2^21 / 2^22 kernels
 
 

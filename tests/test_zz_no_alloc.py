@@ -43,7 +43,7 @@ def _canonical(d: np.ndarray, widths: np.ndarray) -> np.ndarray:
     return np.array(out, dtype=np.uint64)
 
 
-@pytest.mark.parametrize("p,mode", [(1398269, 1), (9437179, 1), (44497, 0)])
+@pytest.mark.parametrize("p,mode", [(1398269, 1), (9437179, 1), (44497, 0), (1398269, 2)])
 def test_noalloc_matches_context_path(m2, p, mode):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
@@ -64,6 +64,36 @@ def test_noalloc_matches_context_path(m2, p, mode):
             got = _canonical(dev.cpu().numpy(), widths)
             want = ref.digits()
             assert np.array_equal(got, want), f"p={p}: no-alloc residue differs after {k} more squarings"
+
+
+@pytest.mark.parametrize("p,mode", [(86243, 1), (756839, 2), (3021377, 0)])
+def test_noalloc_accepts_signed_noncanonical_digits(m2, p, mode):
+    """Any digits with |d_j| < 2^width_j are a valid input: seeded random signed
+    digits over the whole range (including values below -2^(width-1), which the
+    entry point must rebalance before its first squaring) against the context
+    path loaded with the canonical digits of the same residue."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    lib = m2._lib()
+    _, n, widths = m2.layout(p)
+    rng = np.random.default_rng(p)
+    w = widths.astype(np.int64)
+    mag = (rng.random(n) * (2.0 ** w - 1)).astype(np.int64)      # in [0, 2^w - 1)
+    sign = rng.integers(0, 2, n) * 2 - 1
+    start = mag * sign
+    start[:8] = -((1 << w[:8]) - 1)                                 # the extreme negative digits
+    canon = _canonical(start, widths)
+    dev = torch.from_numpy(start.copy()).to("cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    with m2.Engine(p, mode) as ref:
+        ref.set_digits(canon, 0)
+        for k in (20, 31):
+            rc = lib.m2_square_noalloc(p, mode, ctypes.c_void_p(dev.data_ptr()), k, ctypes.c_void_p(stream))
+            assert rc == 0, m2.M2Error(rc, "m2_square_noalloc")
+            ref.iterate(k)
+            got = _canonical(dev.cpu().numpy(), widths)
+            assert np.array_equal(got, ref.digits()), f"p={p} mode={mode}: residue differs after {k} more squarings"
 
 
 def test_noalloc_rejects_out_of_range_sizes(m2):
