@@ -17,6 +17,9 @@ Also reported:
             count against the measured mad.wide.u32 peak
   cpu_baseline  the reference's own kernels on the host cores (oracle/_ref),
             bounded sample
+  reference_opencl_gpu  the reference program itself (mersenne2_gpu.cpp, its
+            OpenCL host code and kernels) on this GPU through the vendor
+            OpenCL driver: ms/iter from its own progress lines
   batched   config "4096 seeded PRP tests, p in [3, 159739]" through the batched
             engine vs one test at a time (sampled), res64 bit-exact
   serving   seeded Poisson stream of PRP requests, p log-uniform in
@@ -272,6 +275,27 @@ def run_reference(a, dist: Dist) -> dict | None:
     }
 
 
+def reference_opencl_gpu(p: int, iters: int) -> dict:
+    """The reference program on this GPU (oracle.ref_opencl_run): its own CLI,
+    `p prp 1000 -N iters`; ms/iter from the elapsed times it prints at the first
+    and the last report (the first 1000 squarings, which include its warm-up,
+    are left out)."""
+    import re
+
+    import oracle
+    rc, out = oracle.ref_opencl_run([str(p), "prp", "1000", "-N", str(iters)], timeout=600)
+    pts = [(int(a), float(b)) for a, b in re.findall(r"iter (\d+)/\d+ .*?elapsed ([0-9.]+) s", out)]
+    pts = [x for x in pts if x[0] >= 1000]
+    if rc != 0 or len(pts) < 2:
+        return {"value": None, "sample": f"unavailable: exit {rc}: {out.strip().splitlines()[-1] if out.strip() else ''}"}
+    (i0, t0), (i1, t1) = pts[0], pts[-1]
+    dev = re.search(r"device=\d+ \(([^)]*)\)", out)
+    return {"value": (t1 - t0) / (i1 - i0) * 1e3, "unit": "ms/iter", "kind": "reference",
+            "device": dev.group(1) if dev else None,
+            "sample": f"mersenne2_gpu.cpp's own OpenCL path on this GPU, squarings {i0}..{i1} of p={p} "
+                      f"(its progress lines, one clFinish per 1000)"}
+
+
 # ---------------------------------------------------------------- n = 2^22
 def run_n22(a, stream) -> dict:
     """Config 3's second exponent: the seeded prime in [73400329, 142606333]
@@ -387,8 +411,8 @@ def run_batched(count: int, plain_sample: int, mul_peak: float | None = None) ->
         "speedup_vs_plain": (tests_per_s / plain_tests_per_s) if (tests_per_s and plain_tests_per_s) else None,
         "bit_exact_vs_plain": f"{same}/{plain_sample}", "buckets": br.buckets, "launches": br.launches,
         "primes_found": int(br.is_prime.sum()), "roofline_imad": roof,
-        "tuned_threads_per_bucket": {f"n=2^{ln}": {"threads": t[0], "ns_per_test_squaring": round(t[1], 1)}
-                                     for ln in range(3, 14) if (t := m2.batch_tuned(ln)) is not None},
+        "tuned_per_bucket": {f"n=2^{ln}": {k: (round(v, 1) if isinstance(v, float) else v) for k, v in t.items()}
+                             for ln in range(3, 15) if (t := m2.batch_tuning(ln)) is not None},
     }
 
 
@@ -536,6 +560,11 @@ def run_gb300(a, dist: Dist) -> dict | None:
             out["cpu_baseline"]["gmp_single_thread"] = gmp_sample(a.p, 3)
         except Exception as ex:  # noqa: BLE001
             out["cpu_baseline"]["gmp_single_thread"] = {"value": None, "sample": f"unavailable: {ex}"}
+    if a.ref_opencl and dist.world == 1:
+        try:
+            out["reference_opencl_gpu"] = reference_opencl_gpu(a.p, 3000)
+        except Exception as ex:  # noqa: BLE001
+            out["reference_opencl_gpu"] = {"value": None, "sample": f"unavailable: {ex}"}
     if a.n22 and dist.world == 1:
         try:
             out["n22"] = run_n22(a, stream)
@@ -572,6 +601,7 @@ def main() -> int:
     ap.add_argument("--profile-iters", type=int, default=50)
     ap.add_argument("--cpu-iters", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-ref-opencl", dest="ref_opencl", action="store_false")
     ap.add_argument("--no-n22", dest="n22", action="store_false")
     ap.add_argument("--n22-iters", type=int, default=2500)
     ap.add_argument("--n22-steps", type=int, default=6)   # (2 + 6) x 2500: checked at GMP's iteration 20000

@@ -60,7 +60,10 @@ typedef struct m2_ctx m2_ctx;
 
 /* Options; zero-initialise and set what you need.  The -W / -B knobs of the
  * reference (mersenne2_gpu.cpp:3668-3680) are accepted: wg is the threads per
- * CTA hint, carry_pairs the carry segment size hint (pairs of digits). */
+ * CTA hint, carry_pairs the carry segment size hint (pairs of digits: on the
+ * one-CTA path n / (2 carry_pairs) segments, rounded to a power of two and
+ * kept within the threads and the carry span; on the three-pass path the
+ * columns per CTA). */
 typedef struct {
     int device;             /* CUDA device ordinal (reference -d, mersenne2_gpu.cpp:3651-3656) */
     uint32_t wg;            /* -W: threads per CTA hint (0 = auto) */
@@ -68,6 +71,9 @@ typedef struct {
     int path;               /* M2_PATH_* */
     void* stream;           /* cudaStream_t to run on (NULL = the context creates one) */
     int fields;             /* M2_FIELDS_* */
+    int fused_middle;       /* one-CTA path: 1 runs the last forward level, the centre square and the first
+                               inverse level as one pass (the reference runs them as separate launches,
+                               mersenne2_gpu.cpp:4512-4531); 0 = separate passes */
 } m2_opts;
 
 typedef struct {
@@ -306,6 +312,33 @@ int m2_batch_run(const uint32_t* p, const int* modes, const uint32_t* iters, siz
  * 32 ... 256 times a sample of the batch's own tests; the carry split follows),
  * and the measured nanoseconds per test-squaring.  M2_EINVAL if not tuned yet. */
 int m2_batch_tuned(int device, int ln, int* threads, double* ns_per_test_iter);
+
+/* The full choice of the batch autotuner for transform size 2^ln on `device`
+ * (M2_EINVAL if not tuned yet).  The tuner times every valid combination of
+ * three knobs on a sample of the batch's own tests:
+ *   threads        threads per transform (the reference's -W work-group size,
+ *                  mersenne2_gpu.cpp:3668-3672), 32 ... 256;
+ *   carry_blocks   segments of the carry, each normalising n / carry_blocks
+ *                  digits serially before handing its carry to the next
+ *                  (the reference's -B carry block of carry_pairs digit pairs,
+ *                  mersenne2_gpu.cpp:3676-3680, 3950-3968): threads, threads/2
+ *                  or threads/4 segments;
+ *   fused_middle   radix split of the transform's middle: 0 runs the last
+ *                  forward level, the centre square and the first inverse level
+ *                  as three shared-memory passes (the reference's separate
+ *                  forward4 / square_half / backward4 launches,
+ *                  mersenne2_gpu.cpp:4512-4531), 1 runs them as one pass over
+ *                  pairs of mirror blocks.
+ * carry_pairs = n / (2 carry_blocks) is the -B value of that choice. */
+typedef struct {
+    int threads;
+    int carry_blocks;
+    int carry_pairs;
+    int fused_middle;
+    double ns_per_test_iter;  /* measured nanoseconds per test-squaring of the choice */
+    double ns_default;        /* the same for the untuned default (h/4 threads, one segment per thread, unfused) */
+} m2_batch_tuning_t;
+int m2_batch_tuning(int device, int ln, m2_batch_tuning_t* out);
 
 #ifdef __cplusplus
 }

@@ -26,7 +26,7 @@ EXPORTS = (
     "m2_verdict", "m2_info", "m2_destroy", "m2_layout", "m2_strerror", "m2_batch_run",
     "m2_profile", "m2_launches_for", "m2_measure_mul_peak", "m2_square_noalloc",
     "m2_srv_create", "m2_srv_submit", "m2_srv_step", "m2_srv_poll", "m2_srv_stats_get", "m2_srv_destroy",
-    "m2_last_error", "m2_carry_normalize", "m2_batch_tuned", "m2_layout_fields", "m2_test_stall_fused",
+    "m2_last_error", "m2_carry_normalize", "m2_batch_tuned", "m2_batch_tuning", "m2_layout_fields", "m2_test_stall_fused",
     "m2_gec_create", "m2_gec_iterate", "m2_gec_check", "m2_gec_verified", "m2_gec_stats_get", "m2_gec_destroy",
 )
 E_CHECK = -7   # M2_ECHECK
@@ -41,7 +41,8 @@ class M2Error(RuntimeError):
 
 class _Opts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("wg", ctypes.c_uint32), ("carry_pairs", ctypes.c_uint32),
-                ("path", ctypes.c_int), ("stream", ctypes.c_void_p), ("fields", ctypes.c_int)]
+                ("path", ctypes.c_int), ("stream", ctypes.c_void_p), ("fields", ctypes.c_int),
+                ("fused_middle", ctypes.c_int)]
 
 
 class _Info(ctypes.Structure):
@@ -60,6 +61,11 @@ class _StageTime(ctypes.Structure):
 class _GecStats(ctypes.Structure):
     _fields_ = [("verified_iter", ctypes.c_uint32), ("block", ctypes.c_uint32), ("updates", ctypes.c_uint64),
                 ("checks", ctypes.c_uint64), ("failures", ctypes.c_uint64), ("seconds", ctypes.c_double)]
+
+
+class _BatchTuning(ctypes.Structure):
+    _fields_ = [("threads", ctypes.c_int), ("carry_blocks", ctypes.c_int), ("carry_pairs", ctypes.c_int),
+                ("fused_middle", ctypes.c_int), ("ns_per_test_iter", ctypes.c_double), ("ns_default", ctypes.c_double)]
 
 
 class _BatchStats(ctypes.Structure):
@@ -100,6 +106,7 @@ def _lib() -> ctypes.CDLL:
         L.m2_carry_normalize.argtypes = [u32, vp, vp, u32, vp, vp]
         L.m2_test_stall_fused.argtypes = [vp]
         L.m2_batch_tuned.argtypes = [i, i, ctypes.POINTER(i), ctypes.POINTER(ctypes.c_double)]
+        L.m2_batch_tuning.argtypes = [i, i, ctypes.POINTER(_BatchTuning)]
         L.m2_last_error.argtypes = []
         L.m2_gec_create.argtypes = [ctypes.POINTER(vp), vp, u32]
         L.m2_gec_iterate.argtypes = [vp, u32]
@@ -157,12 +164,13 @@ class Engine:
     """One test of 2^p - 1 on one GPU (wraps an m2_ctx)."""
 
     def __init__(self, p: int, mode: int | str = MODE_PRP, device: int = 0, path: int = PATH_AUTO,
-                 wg: int = 0, carry_pairs: int = 0, stream: int | None = None, fields: int = FIELDS_DUAL):
+                 wg: int = 0, carry_pairs: int = 0, stream: int | None = None, fields: int = FIELDS_DUAL,
+                 fused_middle: int = 0):
         if isinstance(mode, str):
             mode = _MODES[mode.lower()]
         self._L = _lib()
         self._h = ctypes.c_void_p()
-        o = _Opts(device, wg, carry_pairs, path, stream, fields)
+        o = _Opts(device, wg, carry_pairs, path, stream, fields, fused_middle)
         _check(self._L.m2_create(ctypes.byref(self._h), p, mode, ctypes.byref(o)), f"m2_create(p={p})")
         self.p, self.mode = p, mode
         self.info()
@@ -351,3 +359,16 @@ def batch_tuned(ln: int, device: int = 0) -> tuple[int, float] | None:
     t, ns = ctypes.c_int(), ctypes.c_double()
     rc = _lib().m2_batch_tuned(device, ln, ctypes.byref(t), ctypes.byref(ns))
     return (t.value, ns.value) if rc == 0 else None
+
+
+def batch_tuning(ln: int, device: int = 0) -> dict | None:
+    """The batch autotuner's choice for transform size 2^ln (None if not tuned):
+    threads per transform, carry blocks and their length in digit pairs (-B),
+    fused or separate transform middle, and the measured ns per test-squaring
+    of the choice and of the untuned default."""
+    t = _BatchTuning()
+    if _lib().m2_batch_tuning(device, ln, ctypes.byref(t)) != 0:
+        return None
+    return {"threads": t.threads, "carry_blocks": t.carry_blocks, "carry_pairs": t.carry_pairs,
+            "fused_middle": t.fused_middle, "ns_per_test_squaring": t.ns_per_test_iter,
+            "ns_default": t.ns_default}

@@ -104,11 +104,13 @@ u32 total_iters_for(u32 p, int mode) {
     return p;
 }
 
-// Carry threads of the one-CTA path: a power of two, each owning n/Tc >= span+1
-// digits; 0 selects the single-thread full normalization (tiny exponents).
-int small_carry_threads(const m2::Layout& L, int span, int threads) {
+// Carry threads of the one-CTA path: a power of two (threads >> shift at most),
+// each owning n/Tc >= span+1 digits; 0 selects the single-thread full
+// normalization (tiny exponents).
+int small_carry_threads(const m2::Layout& L, int span, int threads, int shift = 0) {
     if (L.q < 4) return 0;
-    u64 tc = (u64)threads;
+    u64 tc = (u64)(threads >> shift);
+    if (tc < 1) tc = 1;
     while (tc > 1 && L.n / tc < (u64)span + 1) tc >>= 1;
     if (L.n / tc < (u64)span + 1) return 0;
     return (int)tc;
@@ -393,12 +395,21 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
         raw->threads = m2k::small_threads_for((unsigned)h);
         if (o.wg >= 32 && o.wg <= 256 && (o.wg & (o.wg - 1)) == 0) raw->threads = (int)o.wg;
         raw->carry_threads = small_carry_threads(raw->L, raw->span, raw->threads);
+        if (o.carry_pairs > 0 && raw->carry_threads > 0) {
+            // -B: segments of about 2 carry_pairs digits, a power of two of them
+            int shift = 0;
+            while (shift < 8 && (u64)(raw->threads >> (shift + 1)) >= 1 &&
+                   2ull * o.carry_pairs * (u64)(raw->threads >> shift) > n)
+                ++shift;
+            raw->carry_threads = small_carry_threads(raw->L, raw->span, raw->threads, shift);
+        }
         if ((rc = dalloc(raw, &raw->d_test, sizeof(m2k::SmallTest)))) { m2_destroy(c.release()); return rc; }
         m2k::SmallTest t{};
         t.digits = raw->d_digits; t.w61 = raw->d_w61; t.w31 = raw->d_w31;
         t.tw4 = raw->tw.tw4; t.tc = raw->tw.tc; t.status = raw->d_status;
         t.p = p; t.iters = 0; t.ln = raw->L.ln; t.mode = mode; t.span = raw->span;
         t.carry_threads = raw->carry_threads;
+        t.fuse_middle = o.fused_middle ? 1 : 0;
         t.gf61_only = gf61 ? 1 : 0;
         raw->h_test = t;
         if (cudaMemcpyAsync(raw->d_test, &raw->h_test, sizeof(t), cudaMemcpyHostToDevice, raw->stream) != cudaSuccess) {
@@ -434,7 +445,7 @@ int m2_iterate(m2_ctx* c, uint32_t k) {
     if (cudaSetDevice(c->device) != cudaSuccess) return M2_ECUDA;
     cudaError_t e = cudaSuccess;
     if (c->path == M2_PATH_SMALL) {
-        e = m2k::launch_small(c->d_test, 1, (unsigned)c->L.h, c->threads, k, c->stream);
+        e = m2k::launch_small(c->d_test, 1, (unsigned)c->L.h, c->threads, k, c->stream, c->h_test.fuse_middle != 0);
     } else {
         uint32_t left = k;
         if (left >= GRAPH_ITERS && ensure_graph(c))
@@ -624,7 +635,7 @@ int m2_profile(m2_ctx* c, uint32_t iters, m2_stage_time* out, int max_stages, in
     for (auto& e : ev) if (cudaEventCreate(&e) != cudaSuccess) return M2_ECUDA;
     cudaError_t err = cudaEventRecord(ev[0], c->stream);
     for (size_t i = 0; i < seq.size() && err == cudaSuccess; ++i) {
-        if (seq[i] < 0) err = m2k::launch_small(c->d_test, 1, (unsigned)c->L.h, c->threads, iters, c->stream);
+        if (seq[i] < 0) err = m2k::launch_small(c->d_test, 1, (unsigned)c->L.h, c->threads, iters, c->stream, c->h_test.fuse_middle != 0);
         else err = m2k::launch_large_stage(c->plan, c->bufs, seq[i], c->stream);
         if (err == cudaSuccess) err = cudaEventRecord(ev[i + 1], c->stream);
     }
@@ -682,14 +693,20 @@ int m2_measure_mul_peak(int device, double* products_per_s) {
 // ---------------- batched engine ----------------
 namespace {
 
-// Threads per transform of the one-CTA kernel, tuned per (device, h): every
-// candidate (32 ... 256; the segmented carry's split follows from it) runs a
-// GPU-filling sample of the bucket's own tests for TUNE_ITERS squarings on
-// scratch copies of their state, and the highest rate of test-squarings per
-// second wins.  Cached for the process.
-struct Tuned { int threads; double ns_per_test_iter; };
+// Launch shape of the one-CTA kernel, tuned per (device, h): every
+// combination of threads per transform (32 ... 256), carry segments (threads,
+// threads / 2, threads / 4, each segment at least span + 1 digits) and the
+// fused or separate transform middle runs a GPU-filling sample of the bucket's
+// own tests for TUNE_ITERS squarings on scratch copies of their state; the
+// highest rate of test-squarings per second wins.  Cached for the process.
+struct Tuned {
+    int threads = 0, carry_shift = 0, fuse = 0;
+    double ns_per_test_iter = 0.0, ns_default = 0.0;
+    int carry_blocks(const m2::Layout& L, int span) const { return small_carry_threads(L, span, threads, carry_shift); }
+};
 std::mutex g_tune_mu;
 std::map<std::pair<int, u64>, Tuned> g_tune;
+std::map<std::pair<int, u64>, std::pair<int, int>> g_tune_shape;   // (device, h) -> (carry blocks, n) of the choice
 constexpr u32 TUNE_ITERS = 48;
 
 template <class Item>
@@ -720,32 +737,47 @@ int tune_bucket(int device, u64 h, const std::vector<Item>& items, const std::ve
         cleanup();
         return M2_ENOMEM;
     }
-    Tuned best{m2k::small_threads_for((unsigned)h), 0.0};
+    const int T0 = m2k::small_threads_for((unsigned)h);
+    Tuned best;
+    best.threads = T0;
     for (int T = 32; T <= 256; T *= 2) {
-        const int per_sm = m2k::small_ctas_per_sm((unsigned)h, T);
-        const size_t ns = std::min(cap, (size_t)per_sm * (size_t)std::max(sms, 1));
-        std::vector<m2k::SmallTest> d(tests.begin(), tests.begin() + ns);
-        for (size_t t = 0; t < ns; ++t) {
-            d[t].digits = scratch + t * n;
-            d[t].status = d_st;
-            d[t].carry_threads = small_carry_threads(items[t].L, items[t].span, T);
+        for (int shift = 0; shift <= 2; ++shift) {
+            // a carry split that the segment length rules out collapses onto a smaller shift: skip repeats
+            if (shift > 0 && small_carry_threads(items[0].L, items[0].span, T, shift) ==
+                                 small_carry_threads(items[0].L, items[0].span, T, shift - 1))
+                continue;
+            for (int fuse = 0; fuse <= 1; ++fuse) {
+                const int per_sm = m2k::small_ctas_per_sm((unsigned)h, T, fuse != 0);
+                const size_t ns = std::min(cap, (size_t)per_sm * (size_t)std::max(sms, 1));
+                std::vector<m2k::SmallTest> d(tests.begin(), tests.begin() + ns);
+                for (size_t t = 0; t < ns; ++t) {
+                    d[t].digits = scratch + t * n;
+                    d[t].status = d_st;
+                    d[t].carry_threads = small_carry_threads(items[t].L, items[t].span, T, shift);
+                    d[t].fuse_middle = fuse;
+                }
+                cudaError_t e = cudaMemcpyAsync(scratch, d_dig, ns * n * sizeof(i64), cudaMemcpyDeviceToDevice, st);
+                if (e == cudaSuccess) e = cudaMemcpyAsync(d_t, d.data(), ns * sizeof(m2k::SmallTest), cudaMemcpyHostToDevice, st);
+                if (e == cudaSuccess) e = m2k::launch_small(d_t, (int)ns, (unsigned)h, T, 2, st, fuse != 0);   // warm-up
+                if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+                if (e == cudaSuccess) e = m2k::launch_small(d_t, (int)ns, (unsigned)h, T, TUNE_ITERS, st, fuse != 0);
+                if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+                if (e != cudaSuccess) { cleanup(); return fail_cuda("batch tuning", e); }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                const double ns_per = ms * 1e6 / ((double)ns * TUNE_ITERS);
+                if (T == T0 && shift == 0 && fuse == 0) best.ns_default = ns_per;
+                if (best.ns_per_test_iter == 0.0 || ns_per < best.ns_per_test_iter) {
+                    best.threads = T; best.carry_shift = shift; best.fuse = fuse; best.ns_per_test_iter = ns_per;
+                }
+            }
         }
-        cudaError_t e = cudaMemcpyAsync(scratch, d_dig, ns * n * sizeof(i64), cudaMemcpyDeviceToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(d_t, d.data(), ns * sizeof(m2k::SmallTest), cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = m2k::launch_small(d_t, (int)ns, (unsigned)h, T, 2, st);          // warm-up
-        if (e == cudaSuccess) e = cudaEventRecord(e0, st);
-        if (e == cudaSuccess) e = m2k::launch_small(d_t, (int)ns, (unsigned)h, T, TUNE_ITERS, st);
-        if (e == cudaSuccess) e = cudaEventRecord(e1, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) { cleanup(); return fail_cuda("batch tuning", e); }
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        const double ns_per = ms * 1e6 / ((double)ns * TUNE_ITERS);
-        if (best.ns_per_test_iter == 0.0 || ns_per < best.ns_per_test_iter) best = Tuned{T, ns_per};
     }
     cleanup();
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune[{device, h}] = best;
+    g_tune_shape[{device, h}] = {best.carry_blocks(items[0].L, items[0].span), (int)n};
     out = best;
     return M2_OK;
 }
@@ -761,6 +793,22 @@ int m2_batch_tuned(int device, int ln, int* threads, double* ns_per_test_iter) {
     if (it == g_tune.end()) return M2_EINVAL;
     if (threads) *threads = it->second.threads;
     if (ns_per_test_iter) *ns_per_test_iter = it->second.ns_per_test_iter;
+    return M2_OK;
+}
+
+int m2_batch_tuning(int device, int ln, m2_batch_tuning_t* out) {
+    if (ln < 3 || ln > 14 || !out) return M2_EINVAL;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    const u64 h = u64(1) << (ln - 1);
+    auto it = g_tune.find({device, h});
+    auto sh = g_tune_shape.find({device, h});
+    if (it == g_tune.end() || sh == g_tune_shape.end()) return M2_EINVAL;
+    out->threads = it->second.threads;
+    out->carry_blocks = sh->second.first;
+    out->carry_pairs = sh->second.first ? sh->second.second / (2 * sh->second.first) : 0;
+    out->fused_middle = it->second.fuse;
+    out->ns_per_test_iter = it->second.ns_per_test_iter;
+    out->ns_default = it->second.ns_default;
     return M2_OK;
 }
 
@@ -805,7 +853,7 @@ int m2_batch_run(const uint32_t* p, const int* modes, const uint32_t* iters, siz
         dv.allocs.push_back(*ptr);
         return M2_OK;
     };
-    struct Launch { u64 h; int threads; int ntests; int grid; m2k::SmallTest* d_tests; int* d_queue; long long* d_dig; std::vector<Item>* items; };
+    struct Launch { u64 h; int threads; int ntests; int grid; m2k::SmallTest* d_tests; int* d_queue; long long* d_dig; std::vector<Item>* items; bool fuse; };
     std::vector<Launch> launches;
     uint64_t squarings = 0;
     for (auto& kv : buckets) {
@@ -844,13 +892,16 @@ int m2_batch_run(const uint32_t* p, const int* modes, const uint32_t* iters, siz
         Tuned tn;
         if ((rc = tune_bucket(device, h, items, tests, d_dig, sms, tn))) return rc;
         threads = tn.threads;
-        for (size_t t = 0; t < nt; ++t) tests[t].carry_threads = small_carry_threads(items[t].L, items[t].span, threads);
+        for (size_t t = 0; t < nt; ++t) {
+            tests[t].carry_threads = small_carry_threads(items[t].L, items[t].span, threads, tn.carry_shift);
+            tests[t].fuse_middle = tn.fuse;
+        }
         if (cudaMemcpy(d_tests, tests.data(), tests.size() * sizeof(m2k::SmallTest), cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemset(d_q, 0, 2 * sizeof(int)) != cudaSuccess)
             return M2_ECUDA;
-        const int per_sm = m2k::small_ctas_per_sm((unsigned)h, threads);
+        const int per_sm = m2k::small_ctas_per_sm((unsigned)h, threads, tn.fuse != 0);
         const int grid = (int)std::min<size_t>(nt, (size_t)per_sm * (size_t)std::max(sms, 1));
-        launches.push_back(Launch{h, threads, (int)nt, grid, d_tests, d_q, d_dig, &items});
+        launches.push_back(Launch{h, threads, (int)nt, grid, d_tests, d_q, d_dig, &items, tn.fuse != 0});
     }
     // capture: fork from stream 0 to one stream per bucket, join back
     dv.streams.resize(launches.size() + 1);
@@ -864,7 +915,7 @@ int m2_batch_run(const uint32_t* p, const int* modes, const uint32_t* iters, siz
         cudaStream_t sb = dv.streams[b + 1];
         cudaStreamWaitEvent(sb, dv.events[0], 0);
         const Launch& l = launches[b];
-        m2k::launch_small_persistent(l.d_tests, l.ntests, (unsigned)l.h, l.threads, l.d_queue, l.grid, sb);
+        m2k::launch_small_persistent(l.d_tests, l.ntests, (unsigned)l.h, l.threads, l.d_queue, l.grid, sb, l.fuse);
         cudaEventRecord(dv.events[b + 3], sb);
         cudaStreamWaitEvent(s0, dv.events[b + 3], 0);
     }
@@ -1041,11 +1092,14 @@ int srv_launch(m2_server* s) {
         if (rc) return rc;
         b.members = kv.second;
         b.ks.resize(cnt);
+        // one launch per transform size: its first member's kernel variant for all
+        const bool fuse = s->active[kv.second[0]].ctx->h_test.fuse_middle != 0;
         for (size_t j = 0; j < cnt; ++j) {
             SrvItem& it = s->active[kv.second[j]];
             b.ks[j] = std::min(s->quantum, it.total - it.done);
             m2k::SmallTest t = it.ctx->h_test;
             t.iters = b.ks[j];
+            t.fuse_middle = fuse ? 1 : 0;
             t.status = b.d_status + j;
             b.h_tests[j] = t;
         }
@@ -1053,7 +1107,7 @@ int srv_launch(m2_server* s) {
         if (e == cudaSuccess) e = cudaMemcpyAsync(b.d_tests, b.h_tests, cnt * sizeof(m2k::SmallTest), cudaMemcpyHostToDevice, b.stream);
         if (e != cudaSuccess) return fail_cuda("server descriptor upload", e);
         const int threads = s->active[kv.second[0]].ctx->threads;
-        if ((e = m2k::launch_small(b.d_tests, (int)cnt, (unsigned)kv.first, threads, 0u, b.stream)) != cudaSuccess)
+        if ((e = m2k::launch_small(b.d_tests, (int)cnt, (unsigned)kv.first, threads, 0u, b.stream, fuse)) != cudaSuccess)
             return fail_cuda("server small-test launch", e);
         e = cudaMemcpyAsync(b.h_status, b.d_status, cnt * sizeof(int), cudaMemcpyDeviceToHost, b.stream);
         if (e == cudaSuccess) e = cudaEventRecord(b.ev, b.stream);

@@ -102,6 +102,82 @@ __device__ __forceinline__ bool fits64(i128 c) { const i128 hi = c >> 63; return
 // =====================================================================
 // k_small: whole test in one CTA
 // =====================================================================
+
+// The fused middle of a squaring: the last forward level, the centre square and
+// the first inverse level in one pass.  The last level works on blocks of q
+// consecutive positions (q = 4: the last radix-4 step when log2 h is even;
+// q = 2: the radix-2 step when it is odd), and the centre pairs position k
+// with its mirror 3 2^e - k - 1 (2^e <= k < 2^(e+1)), which for k = q j + 2c
+// (j >= 2) lies at offset q - 1 - 2c of block j' = 3 2^e' - 1 - j
+// (2^e' <= j < 2^(e'+1)): blocks j and j' hold each other's mirrors, so one
+// thread runs both blocks through the level, the centre and the inverse level.
+// Blocks 0 and 1 are their own mirrors.  Work item w = 0 is blocks 0 and 1;
+// w >= 1 is the pair j = w + 2^floor(log2 w), j' = 3 2^floor(log2 j) - 1 - j.
+template <int Q>
+__device__ __forceinline__ void fused_middle(const SZ& z, const SmallTest& T, u32 h, u32 s4max) {
+    const u32 nb = h / Q, items = nb > 1 ? nb / 2 : 1;
+    auto fwd = [&](E* x, u32 j) {
+        if (Q == 4) {
+            const u32 ti = 3 * (s4max + j);
+            if (s4max == 1) dif4_1(x[0], x[1], x[2], x[3]);
+            else dif4(x[0], x[1], x[2], x[3], ldtw(T.tw4, ti), ldtw(T.tw4, ti + 1), ldtw(T.tw4, ti + 2));
+        } else {
+            dif2(x[0], x[1], ldtw(T.tc, j));
+        }
+    };
+    auto inv = [&](E* x, u32 j) {
+        if (Q == 4) {
+            const u32 ti = 3 * (s4max + j);
+            if (s4max == 1) dit4_1(x[0], x[1], x[2], x[3]);
+            else dit4(x[0], x[1], x[2], x[3], ldtw(T.tw4, ti), ldtw(T.tw4, ti + 1), ldtw(T.tw4, ti + 2));
+        } else {
+            dit2(x[0], x[1], ldtw(T.tc, j));
+        }
+    };
+    for (u32 w = threadIdx.x; w < items; w += blockDim.x) {
+        E x[Q], y[Q];
+        if (w == 0) {
+            // block 0: positions 0 and 1 are their own mirrors; with q = 4, 2 pairs with 3
+#pragma unroll
+            for (int c = 0; c < Q; ++c) x[c] = z.ld(c);
+            fwd(x, 0);
+            centre_zero(x[0], x[1]);
+            if (Q == 4) centre_pair(x[2], x[3], ldtw(T.tc, 1));
+            inv(x, 0);
+#pragma unroll
+            for (int c = 0; c < Q; ++c) z.st(c, x[c]);
+            if (nb > 1) {
+                // block 1: position Q + 2c pairs with Q + Q - 1 - 2c
+#pragma unroll
+                for (int c = 0; c < Q; ++c) y[c] = z.ld(Q + c);
+                fwd(y, 1);
+#pragma unroll
+                for (int c = 0; c < Q / 2; ++c) centre_pair(y[2 * c], y[Q - 1 - 2 * c], ldtw(T.tc, (Q + 2 * c) / 2));
+                inv(y, 1);
+#pragma unroll
+                for (int c = 0; c < Q; ++c) z.st(Q + c, y[c]);
+            }
+            continue;
+        }
+        const u32 j = w + (1u << (31 - __clz(w)));
+        const u32 jp = (3u << (31 - __clz(j))) - 1u - j;
+#pragma unroll
+        for (int c = 0; c < Q; ++c) { x[c] = z.ld(Q * j + c); y[c] = z.ld(Q * jp + c); }
+        fwd(x, j);
+        fwd(y, jp);
+#pragma unroll
+        for (int c = 0; c < Q / 2; ++c) {
+            centre_pair(x[2 * c], y[Q - 1 - 2 * c], ldtw(T.tc, (Q * j + 2 * c) / 2));
+            centre_pair(y[2 * c], x[Q - 1 - 2 * c], ldtw(T.tc, (Q * jp + 2 * c) / 2));
+        }
+        inv(x, j);
+        inv(y, jp);
+#pragma unroll
+        for (int c = 0; c < Q; ++c) { z.st(Q * j + c, x[c]); z.st(Q * jp + c, y[c]); }
+    }
+}
+
+template <bool FUSE>
 __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, unsigned char* smem) {
     const SZ z = make_sz(smem, h);
     i64* cx = reinterpret_cast<i64*>(smem + 24ull * h);
@@ -111,6 +187,7 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
     const u32 p = T.p;
     const int L = ln - 1;
     const bool odd = (L & 1) != 0;
+    constexpr bool fuse = FUSE;
     u32 s4max = 0;
     for (u32 S = 1; 4 * S <= h; S *= 4) s4max = S;
 
@@ -123,8 +200,10 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
             z.st(k, weigh(d0, d1, T.w61[2 * k], T.w61[2 * k + 1], T.w31[2 * k], T.w31[2 * k + 1]));
         }
         __syncthreads();
-        // forward radix-4 steps, S blocks of M = h/S
-        for (u32 S = 1; S <= s4max && s4max; S *= 4) {
+        // forward radix-4 steps, S blocks of M = h/S (with the fused middle, the
+        // last step of an even log2 h runs there)
+        const u32 s4last = (fuse && !odd) ? s4max / 4 : s4max;
+        for (u32 S = 1; S <= s4last && s4last; S *= 4) {
             const u32 M = h / S, Q = M >> 2;
             for (u32 b = tid; b < h / 4; b += nt) {
                 const u32 j = b / Q, i = b % Q, base = j * M + i;
@@ -136,7 +215,12 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
             }
             __syncthreads();
         }
-        if (odd) {
+        if (fuse) {
+            if (odd) fused_middle<2>(z, T, h, s4max);
+            else fused_middle<4>(z, T, h, s4max);
+            __syncthreads();
+        }
+        if (odd && !fuse) {
             for (u32 b = tid; b < h / 2; b += nt) {
                 E x0 = z.ld(2 * b), x1 = z.ld(2 * b + 1);
                 dif2(x0, x1, ldtw(T.tc, b));
@@ -145,7 +229,7 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
             __syncthreads();
         }
         // centre: even position k with its mirror 3*2^e - k - 1
-        for (u32 b = tid; b < h / 2; b += nt) {
+        for (u32 b = tid; b < h / 2 && !fuse; b += nt) {
             const u32 k = 2 * b;
             if (k == 0) {
                 E z0 = z.ld(0), z1 = z.ld(1);
@@ -159,8 +243,8 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
                 z.st(k, zk); z.st(mk, zm);
             }
         }
-        __syncthreads();
-        if (odd) {
+        if (!fuse) __syncthreads();
+        if (odd && !fuse) {
             for (u32 b = tid; b < h / 2; b += nt) {
                 E x0 = z.ld(2 * b), x1 = z.ld(2 * b + 1);
                 dit2(x0, x1, ldtw(T.tc, b));
@@ -168,7 +252,7 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
             }
             __syncthreads();
         }
-        for (u32 S = s4max; S >= 1 && s4max; S /= 4) {
+        for (u32 S = s4last; S >= 1 && s4last; S /= 4) {
             const u32 M = h / S, Q = M >> 2;
             for (u32 b = tid; b < h / 4; b += nt) {
                 const u32 j = b / Q, i = b % Q, base = j * M + i;
@@ -242,12 +326,15 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
 
 // One CTA per test (queue == nullptr), or a persistent grid whose CTAs take
 // test indices from *queue until all `ntests` are done.
+// FUSE: the transform's middle as one pass (the tests' fuse_middle); a
+// separate instantiation, so that each variant gets its own register budget
+template <bool FUSE>
 __global__ void __launch_bounds__(256, 2) k_small(const SmallTest* tests, int ntests, u32 h, u32 iters_override, int* queue) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_next;
     if (queue == nullptr) {
         const SmallTest T = tests[blockIdx.x];
-        run_small(T, h, iters_override ? iters_override : T.iters, smem);
+        run_small<FUSE>(T, h, iters_override ? iters_override : T.iters, smem);
         return;
     }
     for (;;) {
@@ -257,7 +344,7 @@ __global__ void __launch_bounds__(256, 2) k_small(const SmallTest* tests, int nt
         __syncthreads();
         if (idx >= ntests) break;
         const SmallTest T = tests[idx];
-        run_small(T, h, iters_override ? iters_override : T.iters, smem);
+        run_small<FUSE>(T, h, iters_override ? iters_override : T.iters, smem);
         __syncthreads();
     }
 }
@@ -283,28 +370,35 @@ int small_threads_for(unsigned int h) {
 }
 size_t small_smem_bytes(unsigned int h, int threads) { return 24ull * h + 8ull * (size_t)threads; }
 
-cudaError_t launch_small(const SmallTest* d_tests, int ntests, unsigned int h, int threads, unsigned int iters_override, cudaStream_t s) {
+namespace {
+const void* small_fn(bool fuse) { return fuse ? (const void*)k_small<true> : (const void*)k_small<false>; }
+}  // namespace
+
+cudaError_t launch_small(const SmallTest* d_tests, int ntests, unsigned int h, int threads, unsigned int iters_override,
+                         cudaStream_t s, bool fuse) {
     const size_t sm = small_smem_bytes(h, threads);
-    cudaError_t e = cudaFuncSetAttribute(k_small, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_limit((const void*)k_small));
+    cudaError_t e = cudaFuncSetAttribute(small_fn(fuse), cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_limit(small_fn(fuse)));
     if (e != cudaSuccess) return e;
-    k_small<<<ntests, threads, sm, s>>>(d_tests, ntests, h, iters_override, nullptr);
+    if (fuse) k_small<true><<<ntests, threads, sm, s>>>(d_tests, ntests, h, iters_override, nullptr);
+    else k_small<false><<<ntests, threads, sm, s>>>(d_tests, ntests, h, iters_override, nullptr);
     return cudaGetLastError();
 }
 
 cudaError_t launch_small_persistent(const SmallTest* d_tests, int ntests, unsigned int h, int threads, int* d_queue,
-                                    int grid, cudaStream_t s) {
+                                    int grid, cudaStream_t s, bool fuse) {
     const size_t sm = small_smem_bytes(h, threads);
-    cudaError_t e = cudaFuncSetAttribute(k_small, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_limit((const void*)k_small));
+    cudaError_t e = cudaFuncSetAttribute(small_fn(fuse), cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_limit(small_fn(fuse)));
     if (e != cudaSuccess) return e;
-    k_small<<<grid, threads, sm, s>>>(d_tests, ntests, h, 0u, d_queue);
+    if (fuse) k_small<true><<<grid, threads, sm, s>>>(d_tests, ntests, h, 0u, d_queue);
+    else k_small<false><<<grid, threads, sm, s>>>(d_tests, ntests, h, 0u, d_queue);
     return cudaGetLastError();
 }
 
-int small_ctas_per_sm(unsigned int h, int threads) {
+int small_ctas_per_sm(unsigned int h, int threads, bool fuse) {
     int nb = 0;
     const size_t sm = small_smem_bytes(h, threads);
-    if (cudaFuncSetAttribute(k_small, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_limit((const void*)k_small)) != cudaSuccess) return 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_small, threads, sm) != cudaSuccess) return 1;
+    if (cudaFuncSetAttribute(small_fn(fuse), cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_limit(small_fn(fuse))) != cudaSuccess) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, small_fn(fuse), threads, sm) != cudaSuccess) return 1;
     return nb > 0 ? nb : 1;
 }
 

@@ -28,6 +28,7 @@ struct SmallTest {
     int span;                 // carry span (digits normalized after a segment carry)
     int carry_threads;        // threads taking part in the segmented carry (0 = one thread, full normalization)
     int gf61_only;            // 1: the GF(P61) residue alone is the convolution word (no CRT)
+    int fuse_middle;          // 1: the last forward level, the centre and the first inverse level in one pass
 };
 
 // Plan of the three-pass path for one transform length.
@@ -57,12 +58,15 @@ struct LargeBufs {
 
 size_t small_smem_bytes(unsigned int h, int threads);
 int small_threads_for(unsigned int h);
-// iters_override != 0 replaces every test's iteration count for this launch
-cudaError_t launch_small(const SmallTest* d_tests, int ntests, unsigned int h, int threads, unsigned int iters_override, cudaStream_t s);
+// iters_override != 0 replaces every test's iteration count for this launch;
+// fuse selects the kernel variant with the fused transform middle (every test
+// of the launch must have fuse_middle equal to it)
+cudaError_t launch_small(const SmallTest* d_tests, int ntests, unsigned int h, int threads, unsigned int iters_override,
+                         cudaStream_t s, bool fuse = false);
 // persistent grid: CTAs take test indices from *d_queue (zeroed by the caller)
 cudaError_t launch_small_persistent(const SmallTest* d_tests, int ntests, unsigned int h, int threads, int* d_queue,
-                                    int grid, cudaStream_t s);
-int small_ctas_per_sm(unsigned int h, int threads);
+                                    int grid, cudaStream_t s, bool fuse = false);
+int small_ctas_per_sm(unsigned int h, int threads, bool fuse = false);
 
 size_t large_smem_cols(const LargePlan& P);
 size_t large_smem_rows(const LargePlan& P);

@@ -6,8 +6,10 @@
 // them.  Per CTA:
 //   pass A  levels 1-2 of the row: a 16-element sub-column lives in a quad of
 //           lanes (4 elements each), loaded straight from global memory; one
-//           radix-4 level, an in-quad 4x4 transpose by warp shuffles, the
-//           second radix-4 level, then a store to shared memory;
+//           radix-4 level, then the quad hands its elements over through the
+//           sub-column's own shared-memory slots (store k = l + 4m, warp
+//           barrier, load k = 4l + m), the second radix-4 level, then a store
+//           to shared memory;
 //   pass B  levels 3-4 the same way, shared memory in and out;
 //   tail    the last level (groups of 4, or radix 4 + radix 2 on groups of 8
 //           when log2 B is odd), the centre square and the first inverse

@@ -12,6 +12,10 @@ never imports, links or calls it.
                  (oracle/ref_driver.cpp + oracle/build_ref.py), run in the
                  order of its generic launch plan.
 * python_chain -- exact Python-integer chain for small cases.
+* ref_opencl_run -- the reference program itself on the GPU through the
+                 vendor's OpenCL driver, where one is installed: the timing of
+                 the reference's own GPU path, never a checker of this
+                 engine's digits.
 """
 from __future__ import annotations
 
@@ -27,7 +31,43 @@ LL, PRP, PRP3 = 0, 1, 2
 
 
 def build(reference: str = _build.DEFAULT_REFERENCE) -> tuple[str, str | None]:
-    return _build.build_oracle(), _build.build_ref(reference)
+    out = _build.build_oracle(), _build.build_ref(reference)
+    try:
+        _build.build_ref_opencl(reference)
+    except RuntimeError:
+        pass   # the reference program only serves timing; the CPU oracles above do not depend on it
+    return out
+
+
+# where NVIDIA's driver installs its OpenCL implementation
+_OPENCL_VENDOR_LIBS = ("/usr/lib/libnvidia-opencl.so.1", "/usr/lib64/libnvidia-opencl.so.1",
+                       "/usr/lib/aarch64-linux-gnu/libnvidia-opencl.so.1",
+                       "/usr/lib/x86_64-linux-gnu/libnvidia-opencl.so.1",
+                       "/usr/local/nvidia/lib64/libnvidia-opencl.so.1")
+
+
+def opencl_vendor_lib() -> str | None:
+    for c in _OPENCL_VENDOR_LIBS:
+        if os.path.exists(c):
+            return c
+    return None
+
+
+def ref_opencl_run(args: list[str], timeout: float = 600.0) -> tuple[int, str]:
+    """Runs the reference program (oracle/_ref/mersenne2_ocl) with its own
+    argv `args` on the GPU through the vendor OpenCL driver; returns (exit
+    code, stdout + stderr).  RuntimeError when the program or a driver is
+    missing."""
+    import subprocess
+    exe = _build.build_ref_opencl()
+    if exe is None:
+        raise RuntimeError("reference program not built (reference source absent)")
+    vend = opencl_vendor_lib()
+    if vend is None:
+        raise RuntimeError("no vendor OpenCL driver library on this machine")
+    env = dict(os.environ, M2_OCL_VENDOR_LIB=vend)
+    r = subprocess.run([exe, *args], capture_output=True, text=True, timeout=timeout, env=env)
+    return r.returncode, r.stdout + r.stderr
 
 
 _O = None

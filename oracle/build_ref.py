@@ -1,7 +1,7 @@
 """Build the CPU oracles (test infrastructure only).
 
 1. oracle/m2_oracle.c (the plain-C restatement) -> oracle/_build/liboracle.so
-2. the reference's own kernels -> oracle/_ref/libm2ref.so:
+2. the reference's own kernels -> oracle/_ref/libm2ref.so (for the CPU):
    when the reference checkout is present, the host math (mersenne2_gpu.cpp:75-293)
    and the OpenCL kernel string KC (mersenne2_gpu.cpp:295-3026) are cut out of
    it, by marker, into oracle/_ref/ref_host.inc and oracle/_ref/ref_kernels.inc
@@ -9,6 +9,12 @@
    oracle/ref_driver.cpp is compiled against them.  Where the checkout is
    absent but the .inc files are there (a copy of this tree taken elsewhere),
    only the compile step runs.
+3. the reference program itself, OpenCL host code and all (mersenne2_gpu.cpp,
+   copied whole into oracle/_ref/) -> oracle/_ref/mersenne2_ocl, compiled
+   against the hand-declared OpenCL prototypes of oracle/ocl_min/CL/cl.h and
+   the minimal ICD dispatcher oracle/ocl_min/icd_min.cpp, which reaches the
+   vendor's OpenCL driver at run time (oracle.ref_opencl_run).  It times the
+   reference's own GPU path; building it needs no GPU.
 
 Usage: python oracle/build_ref.py [--reference DIR]
 The reference checkout is DIR, else $M2_REFERENCE, else a directory named
@@ -32,6 +38,9 @@ def extract(reference: str) -> bool:
     if not os.path.isfile(src):
         return False
     text = open(src, encoding="utf-8").read()
+    os.makedirs(REF_DIR, exist_ok=True)
+    with open(os.path.join(REF_DIR, "mersenne2_gpu.cpp"), "w", encoding="utf-8") as f:
+        f.write(text)
     host_begin = text.index("static const uint64_t Z61_p")
     kc_decl = text.index('const char* KC = R"CLC(')
     kc_begin = kc_decl + len('const char* KC = R"CLC(')
@@ -80,12 +89,28 @@ def build_ref(reference: str = DEFAULT_REFERENCE) -> str | None:
     return out
 
 
+def build_ref_opencl(reference: str = DEFAULT_REFERENCE) -> str | None:
+    """The reference program with its OpenCL host path (None without its source)."""
+    extract(reference)
+    src = os.path.join(REF_DIR, "mersenne2_gpu.cpp")
+    if not os.path.isfile(src):
+        return None
+    out = os.path.join(REF_DIR, "mersenne2_ocl")
+    ocl = os.path.join(HERE, "ocl_min")
+    deps = [src, os.path.join(ocl, "CL", "cl.h"), os.path.join(ocl, "icd_min.cpp")]
+    if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
+        return out
+    _run(["g++", "-O2", "-std=c++20", "-w", "-I", ocl, "-o", out, src, os.path.join(ocl, "icd_min.cpp"), "-ldl"])
+    return out
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=DEFAULT_REFERENCE)
     a = ap.parse_args()
     print(build_oracle())
     print(build_ref(a.reference))
+    print(build_ref_opencl(a.reference))
     return 0
 
 

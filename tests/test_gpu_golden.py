@@ -95,10 +95,19 @@ def test_config4_batched_golden_and_plain(m2):
     br = m2.batch_run(ps, iters=iters)
     for i, p in enumerate(ps):
         assert f"{int(br.res64[i]):016x}" == g["res64"][str(p)], p
-    # every bucket was autotuned (threads per transform, 32 ... 256)
+    # every bucket was autotuned over threads per transform (32 ... 256), carry
+    # blocks (threads, threads/2, threads/4) and a fused or separate middle,
+    # and the choice is never slower than the untuned default it also timed
     for ln in sorted({m2.layout(p)[0] for p in ps}):
         t = m2.batch_tuned(ln)
         assert t is not None and t[0] in (32, 64, 128, 256) and t[1] > 0, (ln, t)
+        full_t = m2.batch_tuning(ln)
+        assert full_t is not None and full_t["threads"] == t[0], (ln, full_t)
+        assert full_t["fused_middle"] in (0, 1) and full_t["carry_blocks"] >= 0, (ln, full_t)
+        if full_t["carry_blocks"]:
+            assert full_t["carry_blocks"] <= full_t["threads"], (ln, full_t)
+            assert full_t["carry_pairs"] * 2 * full_t["carry_blocks"] == 1 << ln, (ln, full_t)
+        assert full_t["ns_per_test_squaring"] <= full_t["ns_default"], (ln, full_t)
     # full runs: batched == plain on a spread of exponents (each bucket)
     pick = sorted(set(ps))[:: max(1, len(set(ps)) // 24)]
     full = m2.batch_run(pick)

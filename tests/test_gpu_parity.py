@@ -20,8 +20,9 @@ def _cmp(got, want, what):
 @pytest.mark.parametrize("p", TINY)
 @pytest.mark.parametrize("mode", [0, 1, 2])
 def test_tiny_exponents_full_run(m2, oracle_mod, p, mode):
-    """Tiny p (zero-width digits for p < 8): full runs against exact integers."""
-    with m2.Engine(p, mode) as e:
+    """Tiny p (zero-width digits for p < 8): full runs against exact integers,
+    with the one-CTA kernel's middle fused for every other exponent."""
+    with m2.Engine(p, mode, fused_middle=TINY.index(p) % 2) as e:
         iters = m2.total_iterations(p, mode)
         e.iterate(iters)
         want = oracle_mod.python_chain(p, mode, iters) % ((1 << p) - 1)
@@ -50,9 +51,12 @@ def test_9941_state_every_1000(m2, oracle_mod, mode):
 
 @pytest.mark.parametrize("p", [521, 1279, 2203, 4423, 9689, 21701, 44497, 86243, 132049, 216091])
 @pytest.mark.parametrize("mode", [0, 1])
-def test_small_path_vs_oracle(m2, oracle_mod, p, mode):
+@pytest.mark.parametrize("fused", [0, 1])
+def test_small_path_vs_oracle(m2, oracle_mod, p, mode, fused):
+    """The one-CTA kernel with the transform's middle (last forward level, centre
+    square, first inverse level) as separate passes or fused into one pass."""
     iters = 200 if p < 100000 else 60
-    with m2.Engine(p, mode, path=m2.PATH_SMALL) as e:
+    with m2.Engine(p, mode, path=m2.PATH_SMALL, fused_middle=fused) as e:
         e.iterate(iters)
         got = e.digits()
     o = oracle_mod.Oracle(p, mode)
@@ -198,3 +202,14 @@ def test_fused_wait_runs_out_and_reports_timeout(m2, oracle_mod, p):
     o = oracle_mod.Oracle(p, 1)
     o.iterate(3)
     _cmp(got, o.digits(), "after the timeout")
+
+
+@pytest.mark.parametrize("p,cp", [(9941, 16), (44497, 64), (132049, 256), (216091, 1024)])
+def test_small_path_carry_blocks_vs_oracle(m2, oracle_mod, p, cp):
+    """-B (carry_pairs) on the one-CTA path: fewer, longer carry segments."""
+    with m2.Engine(p, 1, path=m2.PATH_SMALL, carry_pairs=cp, fused_middle=1) as e:
+        e.iterate(100)
+        got = e.digits()
+    o = oracle_mod.Oracle(p, 1)
+    o.iterate(100)
+    _cmp(got, o.digits(), f"small p={p} -B {cp}")
