@@ -43,6 +43,10 @@ import sys
 import threading
 import time
 
+# the serving leg runs each large test on its own stream: 32 hardware work
+# queues (not the default 8) let them overlap; read when CUDA starts
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)

@@ -131,6 +131,12 @@ void m2_destroy(m2_ctx* ctx);
  * by up to `quantum` squarings -- tests of one transform size on the one-CTA
  * path share one persistent launch, larger tests run on their own streams, all
  * concurrently -- then retires the finished tests and frees their memory.
+ * A test is admitted on an estimate of its device memory and then holds the
+ * bytes its context actually allocated (the twiddle tables of a transform size
+ * are shared by every test of that size and cached for the process, outside
+ * the budget).  Shared one-CTA launches take the batch autotuner's launch
+ * shape for their transform size when m2_batch_run has tuned it in this
+ * process, else the default shape.
  * Results of a test are identical to running it alone (m2_create/m2_iterate).
  * Times are seconds since m2_srv_create (host steady clock). */
 typedef struct m2_server m2_server;
@@ -164,6 +170,19 @@ int m2_srv_step(m2_server* s);
 /* copies up to max finished results (oldest first) and removes them */
 int m2_srv_poll(m2_server* s, m2_srv_result* out, int max, int* n_out);
 int m2_srv_stats_get(m2_server* s, m2_srv_stats* st);
+/* progress of the admitted (active) tests, in admission order: up to max of
+ * them, *n_out = how many were written */
+typedef struct {
+    uint64_t id;
+    uint32_t p;
+    uint32_t done;           /* squarings accounted so far */
+    uint32_t total;          /* squarings the test will run */
+    uint32_t inflight;       /* squarings launched and not yet accounted */
+    uint64_t n;              /* transform length */
+    uint64_t device_bytes;   /* device memory the test holds */
+    double t_submit, t_admit;
+} m2_srv_progress;
+int m2_srv_active_get(m2_server* s, m2_srv_progress* out, int max, int* n_out);
 void m2_srv_destroy(m2_server* s);
 
 /* ---------------- profiling ---------------- */

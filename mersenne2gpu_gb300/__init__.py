@@ -25,7 +25,8 @@ EXPORTS = (
     "m2_create", "m2_iterate", "m2_sync", "m2_get_digits", "m2_set_digits", "m2_res64",
     "m2_verdict", "m2_info", "m2_destroy", "m2_layout", "m2_strerror", "m2_batch_run",
     "m2_profile", "m2_launches_for", "m2_measure_mul_peak", "m2_square_noalloc",
-    "m2_srv_create", "m2_srv_submit", "m2_srv_step", "m2_srv_poll", "m2_srv_stats_get", "m2_srv_destroy",
+    "m2_srv_create", "m2_srv_submit", "m2_srv_step", "m2_srv_poll", "m2_srv_stats_get", "m2_srv_active_get",
+    "m2_srv_destroy",
     "m2_last_error", "m2_carry_normalize", "m2_batch_tuned", "m2_batch_tuning", "m2_layout_fields", "m2_test_stall_fused",
     "m2_gec_create", "m2_gec_iterate", "m2_gec_check", "m2_gec_verified", "m2_gec_stats_get", "m2_gec_destroy",
 )

@@ -1092,21 +1092,31 @@ int srv_launch(m2_server* s) {
         if (rc) return rc;
         b.members = kv.second;
         b.ks.resize(cnt);
-        // one launch per transform size: its first member's kernel variant for all
-        const bool fuse = s->active[kv.second[0]].ctx->h_test.fuse_middle != 0;
+        // one launch per transform size: the batch autotuner's shape for it when
+        // cached, else the first member's; every member gets the launch's variant
+        const m2_ctx* c0 = s->active[kv.second[0]].ctx;
+        Tuned tn;
+        bool tuned = false;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            auto f = g_tune.find({s->device, kv.first});
+            if (f != g_tune.end()) { tn = f->second; tuned = true; }
+        }
+        const int threads = tuned ? tn.threads : c0->threads;
+        const bool fuse = tuned ? tn.fuse != 0 : c0->h_test.fuse_middle != 0;
         for (size_t j = 0; j < cnt; ++j) {
             SrvItem& it = s->active[kv.second[j]];
             b.ks[j] = std::min(s->quantum, it.total - it.done);
             m2k::SmallTest t = it.ctx->h_test;
             t.iters = b.ks[j];
             t.fuse_middle = fuse ? 1 : 0;
+            if (tuned) t.carry_threads = small_carry_threads(it.ctx->L, it.ctx->span, threads, tn.carry_shift);
             t.status = b.d_status + j;
             b.h_tests[j] = t;
         }
         cudaError_t e = cudaMemsetAsync(b.d_status, 0, cnt * sizeof(int), b.stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(b.d_tests, b.h_tests, cnt * sizeof(m2k::SmallTest), cudaMemcpyHostToDevice, b.stream);
         if (e != cudaSuccess) return fail_cuda("server descriptor upload", e);
-        const int threads = s->active[kv.second[0]].ctx->threads;
         if ((e = m2k::launch_small(b.d_tests, (int)cnt, (unsigned)kv.first, threads, 0u, b.stream, fuse)) != cudaSuccess)
             return fail_cuda("server small-test launch", e);
         e = cudaMemcpyAsync(b.h_status, b.d_status, cnt * sizeof(int), cudaMemcpyDeviceToHost, b.stream);
@@ -1207,6 +1217,10 @@ int m2_srv_step(m2_server* s) {
         it.t_admit = s->now();
         s->resident += it.bytes;
         if (rc != M2_OK) { it.ctx = nullptr; srv_retire(s, it, rc); continue; }
+        // from now on the test holds what its context allocated (shared tables excluded)
+        const uint64_t own = it.ctx->bytes - it.ctx->tw.bytes;
+        s->resident = s->resident - it.bytes + own;
+        it.bytes = own;
         if (it.total == 0) { srv_retire(s, it, M2_OK); continue; }
         if (it.ctx->path == M2_PATH_LARGE) {
             const cudaError_t e = cudaEventCreateWithFlags(&it.ev, cudaEventDisableTiming);
@@ -1251,6 +1265,22 @@ int m2_srv_stats_get(m2_server* s, m2_srv_stats* st) {
     st->completed = s->completed;
     st->steps = s->steps;
     st->launches = s->launches;
+    return M2_OK;
+}
+
+int m2_srv_active_get(m2_server* s, m2_srv_progress* out, int max, int* n_out) {
+    if (!s || (!out && max > 0)) return M2_EINVAL;
+    int n = 0;
+    for (const auto& kv : s->active) {
+        if (n >= max) break;
+        const SrvItem& it = kv.second;
+        m2_srv_progress& g = out[n++];
+        g.id = it.id; g.p = it.p; g.done = it.done; g.total = it.total; g.inflight = it.inflight;
+        g.n = it.ctx ? it.ctx->L.n : 0;
+        g.device_bytes = it.bytes;
+        g.t_submit = it.t_submit; g.t_admit = it.t_admit;
+    }
+    if (n_out) *n_out = n;
     return M2_OK;
 }
 

@@ -6,19 +6,31 @@ primes in [1000, 18874367] (transform n = 32 ... 2^19).  The server admits
 them while their device memory fits the budget, advances every admitted test
 by a quantum of squarings per step (same-size small tests share one launch;
 larger tests run on their own streams, concurrently), and retires finished
-tests.  Reported: time-to-result p50/p99 per transform size over the requests
-completed inside the window, aggregate squarings/s, and a re-check of every
-completed result against the same test run alone.
+tests.  Reported per transform size: time-to-result p50/p99 over the requests
+completed inside the window, the squarings done and the rate each test got
+(completed and still active ones: a full test at n >= 4096 takes longer than
+the window); overall: aggregate squarings/s, and a re-check of completed
+results against the same tests run alone.
 """
 from __future__ import annotations
 
-import ctypes
-import statistics
-import time
-from dataclasses import dataclass
+import os
 
-from . import MODE_PRP, Engine, _check, _lib
-from .workloads import poisson_arrivals, serve_exponents
+# Every three-pass test of the server runs on its own stream.  The CUDA driver
+# maps streams onto CUDA_DEVICE_MAX_CONNECTIONS hardware work queues (8 unless
+# set), and streams that share a queue serialise; 32, its largest value, let the
+# tests' launches overlap (on a GB300: 130k -> 170k squarings/s in the 20 s
+# seeded serving window).  It is read once, when the process first uses CUDA,
+# so it is set here only if nothing has chosen it yet.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
+import ctypes  # noqa: E402
+import statistics  # noqa: E402
+import time  # noqa: E402
+from dataclasses import dataclass  # noqa: E402
+
+from . import MODE_PRP, Engine, _check, _lib  # noqa: E402
+from .workloads import poisson_arrivals, serve_exponents  # noqa: E402
 
 
 class _SrvResult(ctypes.Structure):
@@ -34,6 +46,12 @@ class _SrvStats(ctypes.Structure):
                 ("steps", ctypes.c_uint32), ("launches", ctypes.c_uint32)]
 
 
+class _SrvProgress(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint64), ("p", ctypes.c_uint32), ("done", ctypes.c_uint32), ("total", ctypes.c_uint32),
+                ("inflight", ctypes.c_uint32), ("n", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64),
+                ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double)]
+
+
 def _bind():
     L = _lib()
     if not getattr(L, "_m2_srv_bound", False):
@@ -43,9 +61,10 @@ def _bind():
         L.m2_srv_step.argtypes = [vp]
         L.m2_srv_poll.argtypes = [vp, ctypes.POINTER(_SrvResult), i, ctypes.POINTER(i)]
         L.m2_srv_stats_get.argtypes = [vp, ctypes.POINTER(_SrvStats)]
+        L.m2_srv_active_get.argtypes = [vp, ctypes.POINTER(_SrvProgress), i, ctypes.POINTER(i)]
         L.m2_srv_destroy.argtypes = [vp]
         L.m2_srv_destroy.restype = None
-        for f in ("m2_srv_create", "m2_srv_submit", "m2_srv_step", "m2_srv_poll", "m2_srv_stats_get"):
+        for f in ("m2_srv_create", "m2_srv_submit", "m2_srv_step", "m2_srv_poll", "m2_srv_stats_get", "m2_srv_active_get"):
             getattr(L, f).restype = i
         L._m2_srv_bound = True
     return L
@@ -98,6 +117,13 @@ class Server:
         return [Result(a.id, a.p, a.mode, a.iters, a.res64, bool(a.is_prime), a.status, a.n, a.t_submit, a.t_admit,
                        a.t_done) for a in arr[: n.value]]
 
+    def active(self, max_tests: int = 4096) -> list[dict]:
+        """Progress of the admitted tests (admission order)."""
+        arr = (_SrvProgress * max_tests)()
+        n = ctypes.c_int()
+        _check(self._L.m2_srv_active_get(self._h, arr, max_tests, ctypes.byref(n)), "m2_srv_active_get")
+        return [{k: getattr(a, k) for k, _ in _SrvProgress._fields_} for a in arr[: n.value]]
+
     def stats(self) -> dict:
         s = _SrvStats()
         _check(self._L.m2_srv_stats_get(self._h, ctypes.byref(s)), "m2_srv_stats_get")
@@ -138,12 +164,27 @@ def run_serving(rate_per_s: float = 4.0, window_s: float = 20.0, budget_bytes: i
         elapsed = time.perf_counter() - t0
         st = srv.stats()
         squarings = st["squarings"] - sq0
-    buckets: dict[int, list[float]] = {}
+        active = srv.active()
+    # server clock at the end of the window: the latest time it reported, or the
+    # host window (the server was created just before t0)
+    t_end = max([elapsed] + [r.t_done for r in done])
+    buckets: dict[int, dict] = {}
     for r in done:
         if r.status == 0:
-            buckets.setdefault(r.n, []).append(r.t_done - r.t_submit)
-    per_n = {str(n): {"completed": len(v), "p50_s": _pct(v, 0.50), "p99_s": _pct(v, 0.99)}
-             for n, v in sorted(buckets.items())}
+            b = buckets.setdefault(r.n, {"lat": [], "rates": [], "squarings": 0, "active": 0})
+            b["lat"].append(r.t_done - r.t_submit)
+            b["rates"].append(r.iters / max(1e-9, r.t_done - r.t_admit))
+            b["squarings"] += r.iters
+    for a in active:
+        b = buckets.setdefault(a["n"], {"lat": [], "rates": [], "squarings": 0, "active": 0})
+        b["active"] += 1
+        b["squarings"] += a["done"]
+        if t_end > a["t_admit"]:
+            b["rates"].append(a["done"] / (t_end - a["t_admit"]))
+    per_n = {str(n): {"completed": len(b["lat"]), "p50_s": _pct(b["lat"], 0.50), "p99_s": _pct(b["lat"], 0.99),
+                      "still_active": b["active"], "squarings": b["squarings"],
+                      "squarings_per_s_per_test": statistics.fmean(b["rates"]) if b["rates"] else None}
+             for n, b in sorted(buckets.items())}
     lat = [r.t_done - r.t_submit for r in done if r.status == 0]
     out = {
         "config": f"Poisson arrivals {rate_per_s}/s (seed 5), full PRP tests, p log-uniform over primes in "

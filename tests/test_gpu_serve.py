@@ -41,6 +41,11 @@ def test_server_budget_limits_admission(m2):
         srv.step()
         st = srv.stats()
         assert 0 < st["active"] <= 4 and st["queued"] > 0 and st["resident_bytes"] <= 13_000
+        # the admitted tests hold their contexts' real allocations, which add up to the resident bytes
+        act = srv.active()
+        assert len(act) == st["active"] and all(a["device_bytes"] > 0 and a["n"] == 256 for a in act)
+        assert sum(a["device_bytes"] for a in act) == st["resident_bytes"]
+        assert all(a["done"] + a["inflight"] <= a["total"] == 300 for a in act)
         got = []
         for _ in range(1000):
             srv.step()
