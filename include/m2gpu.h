@@ -252,6 +252,22 @@ int m2_carry_normalize(uint32_t p, const int64_t* digits, const int64_t* seg_car
  * the flags).  M2_EUNSUPPORTED when the context has no fused column pass. */
 int m2_test_stall_fused(m2_ctx* ctx);
 
+/* Test hook for stage-by-stage checks of the three-pass path: runs one stage
+ * of a squaring on the context's state -- 0: the forward column pass (pending
+ * carries, weights, the first log2 R levels of the transform down the columns),
+ * 1: the row pass (the remaining forward levels, the centre square, the first
+ * inverse levels), 2: the inverse column pass (the last inverse levels,
+ * unweight, CRT, carry) -- and copies the transform elements it leaves (h
+ * GF(P61^2) pairs of 64-bit words to za_out, h GF(P31^2) pairs of 32-bit words
+ * to zb_out; either may be NULL), element r B + c holding row r, column c.
+ * Stages 0, 1, 2 in that order make one squaring (stage 2 counts it); between
+ * them the digit state is meaningless.  Blocking.  M2_EUNSUPPORTED on the
+ * one-CTA path.  The reference's host self-tests compare its fused kernels with
+ * its generic chain (mersenne2_gpu.cpp:3200-3240, 3359-3397); this engine's
+ * transform uses its own roots and plan, so its stages are checked against an
+ * exact model of the arithmetic each stage must perform. */
+int m2_test_stage(m2_ctx* ctx, int stage, void* za_out, void* zb_out);
+
 /* ---------------- Gerbicz error check (PRP) ----------------
  * A periodic self-check of a PRP chain (M2_MODE_PRP: x <- x^2 from 3), with
  * rollback to the last verified state.  No reference counterpart: the

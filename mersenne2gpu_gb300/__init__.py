@@ -28,6 +28,7 @@ EXPORTS = (
     "m2_srv_create", "m2_srv_submit", "m2_srv_step", "m2_srv_poll", "m2_srv_stats_get", "m2_srv_active_get",
     "m2_srv_destroy",
     "m2_last_error", "m2_carry_normalize", "m2_batch_tuned", "m2_batch_tuning", "m2_layout_fields", "m2_test_stall_fused",
+    "m2_test_stage",
     "m2_gec_create", "m2_gec_iterate", "m2_gec_check", "m2_gec_verified", "m2_gec_stats_get", "m2_gec_destroy",
 )
 E_CHECK = -7   # M2_ECHECK
@@ -106,6 +107,7 @@ def _lib() -> ctypes.CDLL:
         L.m2_square_noalloc.argtypes = [u32, i, vp, u32, vp]
         L.m2_carry_normalize.argtypes = [u32, vp, vp, u32, vp, vp]
         L.m2_test_stall_fused.argtypes = [vp]
+        L.m2_test_stage.argtypes = [vp, i, vp, vp]
         L.m2_batch_tuned.argtypes = [i, i, ctypes.POINTER(i), ctypes.POINTER(ctypes.c_double)]
         L.m2_batch_tuning.argtypes = [i, i, ctypes.POINTER(_BatchTuning)]
         L.m2_last_error.argtypes = []
@@ -231,6 +233,16 @@ class Engine:
         v = ctypes.c_int()
         _check(self._L.m2_verdict(self._h, ctypes.byref(v)), "m2_verdict")
         return bool(v.value)
+
+    def test_stage(self, stage: int) -> tuple[np.ndarray, np.ndarray]:
+        """Runs one stage of a squaring (three-pass path; m2_test_stage) and
+        returns the transform elements it leaves: (h, 2) uint64 GF(P61^2) and
+        (h, 2) uint32 GF(P31^2) coordinates, element r B + c."""
+        h = self.n // 2
+        za = np.zeros((h, 2), dtype=np.uint64)
+        zb = np.zeros((h, 2), dtype=np.uint32)
+        _check(self._L.m2_test_stage(self._h, stage, za.ctypes.data, zb.ctypes.data), f"m2_test_stage({stage})")
+        return za, zb
 
     def profile(self, iters: int) -> list[dict]:
         """Per-stage average device time over `iters` squarings (advances the state)."""

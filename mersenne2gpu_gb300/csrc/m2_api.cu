@@ -588,6 +588,20 @@ int m2_test_stall_fused(m2_ctx* c) {
     return e == cudaSuccess ? M2_OK : fail_cuda("m2_test_stall_fused", e);
 }
 
+int m2_test_stage(m2_ctx* c, int stage, void* za_out, void* zb_out) {
+    if (!c || stage < 0 || stage > 2) return M2_EINVAL;
+    if (c->path != M2_PATH_LARGE) return M2_EUNSUPPORTED;
+    if (cudaSetDevice(c->device) != cudaSuccess) return M2_ECUDA;
+    cudaError_t e = m2k::launch_large_stage(c->plan, c->bufs, stage, c->stream);
+    const size_t h = c->L.h;
+    if (e == cudaSuccess && za_out) e = cudaMemcpyAsync(za_out, c->d_za, 16 * h, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && zb_out) e = cudaMemcpyAsync(zb_out, c->d_zb, 8 * h, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return fail_cuda("m2_test_stage", e);
+    if (stage == 2) c->iteration += 1;
+    return m2_sync(c);
+}
+
 int m2_info(m2_ctx* c, m2_info_t* info) {
     if (!c || !info) return M2_EINVAL;
     std::memset(info, 0, sizeof(*info));
