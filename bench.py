@@ -46,6 +46,10 @@ import time
 # the serving leg runs each large test on its own stream: 32 hardware work
 # queues (not the default 8) let them overlap; read when CUDA starts
 os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+# the CPU rows (the reference's kernels under OpenMP) pin one thread per core,
+# in both arms, so that their figures are comparable
+os.environ.setdefault("OMP_PROC_BIND", "close")
+os.environ.setdefault("OMP_PLACES", "cores")
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
@@ -268,7 +272,9 @@ def run_reference(a, dist: Dist) -> dict | None:
     dt = time.perf_counter() - t0
     ms_iter = dt / (a.steps * per) * 1e3
     threads = oracle.RefKernels.threads()
-    sample = f"{a.steps} steps x {per} squarings of p={a.p} (n=2^21) through the reference's generic kernel plan"
+    sample = (f"{a.steps} steps x {per} squarings of p={a.p} (n=2^21) through the reference's generic kernel plan, "
+              f"{threads} OpenMP threads (OMP_PROC_BIND={os.environ.get('OMP_PROC_BIND')}, "
+              f"OMP_PLACES={os.environ.get('OMP_PLACES')})")
     return {
         "impl": "reference", "metric": METRIC, "value": ms_iter, "unit": "ms/iter", "n_gpus": a.gpus,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": dt / a.steps * 1e3, "higher_is_better": False,
@@ -549,7 +555,9 @@ def run_gb300(a, dist: Dist) -> dict | None:
             ms, thr, setup = reference_sample(a.p, a.cpu_iters)
             out["cpu_baseline"] = {"value": ms, "unit": "ms/iter", "cores": thr, "kind": "reference",
                                    "sample": f"{a.cpu_iters} squarings of p={a.p} (n=2^21) through the reference's "
-                                             f"own kernels on the host cores (table setup {setup:.1f} s untimed)"}
+                                             f"own kernels on the host cores, {thr} OpenMP threads "
+                                             f"(OMP_PROC_BIND={os.environ.get('OMP_PROC_BIND')}, "
+                                             f"OMP_PLACES={os.environ.get('OMP_PLACES')}; table setup {setup:.1f} s untimed)"}
             try:
                 out["cpu_baseline"]["single_thread"] = {
                     "value": reference_single_thread(a.p, 2), "unit": "ms/iter", "cores": 1, "kind": "reference",
@@ -601,9 +609,9 @@ def main() -> int:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--p", type=int, default=DEFAULT_P)
     ap.add_argument("--iters-per-step", type=int, default=1000)
-    ap.add_argument("--ref-iters-per-step", type=int, default=2)
+    ap.add_argument("--ref-iters-per-step", type=int, default=40)
     ap.add_argument("--profile-iters", type=int, default=50)
-    ap.add_argument("--cpu-iters", type=int, default=8)
+    ap.add_argument("--cpu-iters", type=int, default=400)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-ref-opencl", dest="ref_opencl", action="store_false")
     ap.add_argument("--no-n22", dest="n22", action="store_false")
