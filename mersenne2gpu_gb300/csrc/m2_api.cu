@@ -167,9 +167,9 @@ template <class T> int dalloc(m2_ctx* c, T** p, size_t bytes) {
     return M2_OK;
 }
 
-// the fused column kernel's G epoch flags followed by its 64-bit ticket
-// counter (G is even, so the counter is 8-byte aligned)
-size_t flags_bytes(const m2k::LargePlan& P) { return sizeof(unsigned) * ((size_t)P.G + 2); }
+// the fused column kernel's G epoch flags followed by its 64-bit ticket and
+// phase counters (G is even, so the counters are 8-byte aligned)
+size_t flags_bytes(const m2k::LargePlan& P) { return sizeof(unsigned) * ((size_t)P.G + 4); }
 
 
 // Iterations of the three-pass path per graph replay: 3 kernel nodes each.
@@ -431,7 +431,10 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
         if (m2k::large_setup(P) != cudaSuccess) { m2_destroy(c.release()); return M2_EUNSUPPORTED; }
         raw->fused = m2k::cols_mid_supported(P);
         raw->plan.mid_tickets = (raw->fused && !m2k::cols_mid_cooperative(P)) ? 1u : 0u;
+        // the phase barrier measured faster with R = 1024 rows only (n = 2^21)
+        raw->plan.mid_barrier = (raw->fused && !P.mid_tickets && P.R == 1024u) ? 1u : 0u;
         raw->bufs.ticket = reinterpret_cast<unsigned long long*>(raw->d_flags + P.G);
+        raw->bufs.phase = reinterpret_cast<unsigned long long*>(raw->d_flags + P.G + 2);
     }
     raw->bytes += raw->tw.bytes;
     if ((rc = upload_state(raw, m2::digits_of_small(raw->L, mode == M2_MODE_LL ? 4 : 3)))) { m2_destroy(c.release()); return rc; }

@@ -388,6 +388,11 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* a) {
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
     return v;
 }
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long* a) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(a) : "memory");
+    return v;
+}
 __device__ __forceinline__ void st_release(unsigned* a, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(a), "r"(v) : "memory");
 }
@@ -423,6 +428,10 @@ __global__ void __launch_bounds__(ColShape<CR>::CNT, 65536 / (64 * ColShape<CR>:
 // predecessor's flag; a wait that runs out sets ST_WAIT_TIMEOUT and the CTA
 // goes on.
 //  * TK = false: launched cooperatively, all G CTAs resident, CTA g is group g.
+//    With P.mid_barrier the CTA then also waits until all G groups have
+//    published (a count of arrivals): a CTA alone on its SM then no longer
+//    starts its forward half while CTAs that share an SM are still in their
+//    inverse halves, and those get the SM's issue slots to themselves.
 //  * TK = true: G CTAs that need not all fit at once (G = 512 at n = 2^22).
 //    Each CTA takes its group from a 64-bit ticket counter in arrival order
 //    (ticket t of a launch is group t mod G: every launch draws exactly G).
@@ -455,6 +464,17 @@ __global__ void __launch_bounds__(ColShape<CR>::CNT, 65536 / (64 * ColShape<CR>:
     if (threadIdx.x == 0) {
         const unsigned ep = s_epoch;
         st_release(bf.flags + g, ep);
+        if (!TK && P.mid_barrier) {
+            // phase barrier (cooperative launch, all G CTAs resident): wait
+            // until every group has published.  Every launch adds G, so the
+            // count reaches a multiple of G.
+            const unsigned long long old = atomicAdd(bf.phase, 1ull), target = (old / G + 1) * G;
+            unsigned it = 0;
+            while ((long long)(ld_acquire64(bf.phase) - target) < 0) {
+                if (++it > (1u << 20)) { atomicOr(bf.status, ST_WAIT_TIMEOUT); break; }
+                __nanosleep(128);
+            }
+        }
         const unsigned* prev = bf.flags + (g + G - 1) % G;
         unsigned it = 0;
         while ((int)(ld_acquire(prev) - ep) < 0) {

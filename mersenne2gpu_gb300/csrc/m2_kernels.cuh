@@ -40,6 +40,7 @@ struct LargePlan {
     int mode;
     unsigned int mid_tickets;  // fused column kernel: 0 = cooperative (CTA index = group), 1 = groups by arrival ticket
     unsigned int gf61;         // 1: the GF(P61^2)-only layout; each word is the signed GF(P61) residue (no CRT)
+    unsigned int mid_barrier;  // cooperative fused column kernel: 1 = all groups publish before any goes on
 };
 
 struct LargeBufs {
@@ -52,8 +53,9 @@ struct LargeBufs {
     const DTw* tw4;
     const DTw* tc;
     int* status;
-    unsigned int* flags;      // G epoch flags of the fused column kernel, then its 64-bit ticket counter (zero-initialised)
-    unsigned long long* ticket;
+    unsigned int* flags;      // G epoch flags of the fused column kernel, then its 64-bit ticket counter and
+    unsigned long long* ticket;   // its 64-bit phase counter (zero-initialised)
+    unsigned long long* phase;
 };
 
 size_t small_smem_bytes(unsigned int h, int threads);

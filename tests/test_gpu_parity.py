@@ -183,7 +183,8 @@ def test_gf61_only_n2_22_against_gmp(m2):
             assert f"{e.res64():016x}" == g[name]["1000"], name
 
 
-@pytest.mark.parametrize("p", [18874367, 115640321])   # cooperative launch; groups by arrival ticket (n = 2^22)
+# cooperative launch (n = 2^19), cooperative with the phase barrier (n = 2^21), groups by arrival ticket (n = 2^22)
+@pytest.mark.parametrize("p", [18874367, 57885161, 115640321])
 def test_fused_wait_runs_out_and_reports_timeout(m2, oracle_mod, p):
     """Failure detection without a GPU fault: the fused column kernel's flag
     wait is made to run out (group 0's epoch raised past anything its
