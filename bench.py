@@ -311,15 +311,24 @@ def run_n22(a, stream) -> dict:
     """Config 3's second exponent: the seeded prime in [73400329, 142606333]
     (transform n = 2^22), ms/iter device-timed like the headline (L2 flushed
     between steps), res64 checked against GMP at the golden checkpoints."""
+    from mersenne2gpu_gb300.workloads import large_n22_exponent
+    return run_one(large_n22_exponent(), 0, a.n22_iters, a.n22_steps, 2, stream)
+
+
+def run_gf61_only(a, stream) -> dict:
+    """The headline exponent in the GF(P61^2)-only layout (the GF61 prototype's
+    size rule: n = 2^22 for p = 57885161), timed and checked like n22: the
+    same residues as the dual-field transform, with twice the digits."""
+    return run_one(a.p, 1, 1000, 2, 1, stream)
+
+
+def run_one(p, fields, ips, steps, warm, stream) -> dict:
     import torch
 
     import mersenne2gpu_gb300 as m2
-    from mersenne2gpu_gb300.workloads import large_n22_exponent
-    p = large_n22_exponent()
-    ips, steps, warm = a.n22_iters, a.n22_steps, 2
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=stream.device)
     want = {int(k): v for k, v in ((_load_json(GOLDEN_LARGE) or {}).get(str(p), {}).get("prp", {})).items()}
-    with m2.Engine(p, m2.MODE_PRP, device=stream.device.index or 0, stream=stream.cuda_stream) as eng:
+    with m2.Engine(p, m2.MODE_PRP, device=stream.device.index or 0, stream=stream.cuda_stream, fields=fields) as eng:
         info = eng.info()
         for _ in range(warm):
             flush.zero_()
@@ -337,7 +346,8 @@ def run_n22(a, stream) -> dict:
         if done in want:
             parity = "ok" if f"{eng.res64():016x}" == want[done] else "MISMATCH"
         stages = eng.profile(20)
-    return {"p": p, "n": info.n, "ms_per_iter": ms, "iters": steps * ips, "warmup_iters": warm * ips,
+    return {"p": p, "n": info.n, "fields": "gf61" if fields else "dual", "ms_per_iter": ms, "iters": steps * ips,
+            "warmup_iters": warm * ips,
             "plan": {"rows": info.rows, "row_len": info.row_len, "cols_per_cta": info.cols_per_cta,
                      "fused_cols": info.fused_cols},
             f"res64@{done}": parity,
@@ -582,6 +592,11 @@ def run_gb300(a, dist: Dist) -> dict | None:
             out["n22"] = run_n22(a, stream)
         except Exception as ex:  # noqa: BLE001
             out["n22"] = {"error": str(ex)}
+    if a.gf61 and dist.world == 1:
+        try:
+            out["gf61_only"] = run_gf61_only(a, stream)
+        except Exception as ex:  # noqa: BLE001
+            out["gf61_only"] = {"error": str(ex)}
     if a.gec and dist.world == 1:
         try:
             out["gerbicz"] = run_gec(a, stream)
@@ -615,6 +630,7 @@ def main() -> int:
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-ref-opencl", dest="ref_opencl", action="store_false")
     ap.add_argument("--no-n22", dest="n22", action="store_false")
+    ap.add_argument("--no-gf61", dest="gf61", action="store_false")
     ap.add_argument("--n22-iters", type=int, default=2500)
     ap.add_argument("--n22-steps", type=int, default=6)   # (2 + 6) x 2500: checked at GMP's iteration 20000
     ap.add_argument("--no-gec", dest="gec", action="store_false")
