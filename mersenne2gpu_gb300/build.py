@@ -23,6 +23,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["m2_kernels.cu", "m2_rows.cu", "m2_cols.cu", "m2_carry.cu", "m2_api.cu", "m2_peaks.cu", "m2_noalloc.cu",
               "m2_gec.cu"]
 CXX_SOURCES = ["m2_host.cpp"]
+# the transform kernels, built a second time for the GF(P61^2)-only layout
+# (-DM2_DUAL=0: namespace m2k_g61, the GF(P31^2) half compiled away)
+GF61_SOURCES = ["m2_kernels.cu", "m2_rows.cu", "m2_cols.cu"]
 
 
 def nvcc() -> str:
@@ -51,16 +54,17 @@ def _stale(out: str, deps: list[str]) -> bool:
 def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     nv = nvcc()
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".hpp", ".h"))]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".hpp", ".h", ".inc"))]
     headers.append(os.path.join(ROOT, "include", "m2gpu.h"))
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", CSRC, "-I", os.path.join(ROOT, "include")]
     jobs = []
     objs = []
-    for src in CU_SOURCES:
+    units = [(src, src + ".o", []) for src in CU_SOURCES] + [(src, src + ".g61.o", ["-DM2_DUAL=0"]) for src in GF61_SOURCES]
+    for src, obj, defs in units:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(BUILD, obj)
         objs.append(o)
-        cmd = [nv, *ARCH, "-lineinfo", *common, "--expt-relaxed-constexpr", "-c", s, "-o", o]
+        cmd = [nv, *ARCH, "-lineinfo", *common, *defs, "--expt-relaxed-constexpr", "-c", s, "-o", o]
         if ptxas_info:
             cmd += ["-Xptxas", "-v"]
         if force or ptxas_info or _stale(o, [s, *headers]):

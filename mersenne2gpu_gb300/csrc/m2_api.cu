@@ -448,7 +448,7 @@ int m2_iterate(m2_ctx* c, uint32_t k) {
     if (cudaSetDevice(c->device) != cudaSuccess) return M2_ECUDA;
     cudaError_t e = cudaSuccess;
     if (c->path == M2_PATH_SMALL) {
-        e = m2k::launch_small(c->d_test, 1, (unsigned)c->L.h, c->threads, k, c->stream, c->h_test.fuse_middle != 0);
+        e = m2k::launch_small(c->d_test, 1, (unsigned)c->L.h, c->threads, k, c->stream, c->h_test.fuse_middle != 0, c->gf61);
     } else {
         uint32_t left = k;
         if (left >= GRAPH_ITERS && ensure_graph(c))
@@ -652,7 +652,8 @@ int m2_profile(m2_ctx* c, uint32_t iters, m2_stage_time* out, int max_stages, in
     for (auto& e : ev) if (cudaEventCreate(&e) != cudaSuccess) return M2_ECUDA;
     cudaError_t err = cudaEventRecord(ev[0], c->stream);
     for (size_t i = 0; i < seq.size() && err == cudaSuccess; ++i) {
-        if (seq[i] < 0) err = m2k::launch_small(c->d_test, 1, (unsigned)c->L.h, c->threads, iters, c->stream, c->h_test.fuse_middle != 0);
+        if (seq[i] < 0)
+            err = m2k::launch_small(c->d_test, 1, (unsigned)c->L.h, c->threads, iters, c->stream, c->h_test.fuse_middle != 0, c->gf61);
         else err = m2k::launch_large_stage(c->plan, c->bufs, seq[i], c->stream);
         if (err == cudaSuccess) err = cudaEventRecord(ev[i + 1], c->stream);
     }

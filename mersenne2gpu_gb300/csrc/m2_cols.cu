@@ -22,9 +22,9 @@
 #include "m2_field.cuh"
 #include "m2_kernels.cuh"
 
-using namespace m2d;
+using namespace M2D_NS;
 
-namespace m2k {
+namespace M2K_NS {
 
 namespace {
 
@@ -51,10 +51,11 @@ __device__ __forceinline__ u32 swzc(u32 e) {
 struct S6c {
     u32 *al, *ah, *bl, *bh, *c, *d;
     __device__ __forceinline__ E ldp(u32 p) const {
-        return E{(u64)al[p] | ((u64)ah[p] << 32), (u64)bl[p] | ((u64)bh[p] << 32), c[p], d[p]};
+        return E{(u64)al[p] | ((u64)ah[p] << 32), (u64)bl[p] | ((u64)bh[p] << 32), kDual ? c[p] : 0u, kDual ? d[p] : 0u};
     }
     __device__ __forceinline__ void stp(u32 p, const E& v) const {
-        al[p] = (u32)v.a; ah[p] = (u32)(v.a >> 32); bl[p] = (u32)v.b; bh[p] = (u32)(v.b >> 32); c[p] = v.c; d[p] = v.d;
+        al[p] = (u32)v.a; ah[p] = (u32)(v.a >> 32); bl[p] = (u32)v.b; bh[p] = (u32)(v.b >> 32);
+        if (kDual) { c[p] = v.c; d[p] = v.d; }
     }
     __device__ __forceinline__ E ld(u32 e) const { return ldp(swzc(e)); }
     __device__ __forceinline__ void st(u32 e, const E& v) const { stp(swzc(e), v); }
@@ -66,7 +67,7 @@ __device__ __forceinline__ S6c make_s6c(unsigned char* base, u32 ne) {
 
 __device__ __forceinline__ E ldw(const DTw* t, u64 i) {
     const u64* q = reinterpret_cast<const u64*>(t + i);
-    const u64 a = __ldg(q), b = __ldg(q + 1), cd = __ldg(q + 2);
+    const u64 a = __ldg(q), b = __ldg(q + 1), cd = kDual ? __ldg(q + 2) : 0ull;
     return E{a, b, (u32)cd, (u32)(cd >> 32)};
 }
 struct Tri { E r1, r2, r3; };
@@ -78,7 +79,7 @@ __device__ __forceinline__ Tri tri(const DTw* tw4, u64 S, u64 J) {
 __device__ __forceinline__ u64 bitpos(u32 p, int ln, u64 j) { return j ? ((((u64)p * j) - 1) >> ln) + 1 : 0; }
 __device__ __forceinline__ u32 width_of(u32 p, int ln, u64 j) { return (u32)(bitpos(p, ln, j + 1) - bitpos(p, ln, j)); }
 __device__ __forceinline__ E weigh(i64 d0, i64 d1, u32 s061, u32 s161, u32 s031, u32 s131) {
-    return E{rotl61(digit_to61(d0), s061), rotl61(digit_to61(d1), s161), rotl31(digit_to31(d0), s031), rotl31(digit_to31(d1), s131)};
+    return E{rotl61(digit_to61(d0), s061), rotl61(digit_to61(d1), s161), g31(rotl31(digit_to31(d0), s031)), g31(rotl31(digit_to31(d1), s131))};
 }
 __device__ __forceinline__ u32 unrot61(u32 s, int ln) { const u32 t = (s + (u32)ln + 1u) % 61u; return t ? 61u - t : 0u; }
 __device__ __forceinline__ u32 unrot31(u32 s, int ln) { const u32 t = (s + (u32)ln + 1u) % 31u; return t ? 31u - t : 0u; }
@@ -266,7 +267,7 @@ __device__ __forceinline__ void fwd_passes(const S6c& z, const LargePlan& P, con
             for (int b = 0; b < 4; ++b) {
                 const u64 e = (u64)(4 * J + b) * B + (u64)g * CC + c;
                 bf.za[e] = make_ulonglong2(x[b].a, x[b].b);
-                bf.zb[e] = make_uint2(x[b].c, x[b].d);
+                if (kDual) bf.zb[e] = make_uint2(x[b].c, x[b].d);
             }
         }
     } else {
@@ -275,7 +276,7 @@ __device__ __forceinline__ void fwd_passes(const S6c& z, const LargePlan& P, con
             const E v = z.ld(e);
             const u64 o = (u64)(e / CC) * B + (u64)g * CC + e % CC;
             bf.za[o] = make_ulonglong2(v.a, v.b);
-            bf.zb[o] = make_uint2(v.c, v.d);
+            if (kDual) bf.zb[o] = make_uint2(v.c, v.d);
         }
     }
 }
@@ -296,7 +297,7 @@ __device__ __forceinline__ void inv_passes(const S6c& z, const LargePlan& P, con
             for (int b = 0; b < 4; ++b) {
                 const u64 e = (u64)(4 * J + b) * B + (u64)g * CC + c;
                 const ulonglong2 va = bf.za[e];
-                const uint2 vb = bf.zb[e];
+                const uint2 vb = kDual ? bf.zb[e] : make_uint2(0u, 0u);
                 x[b] = E{va.x, va.y, vb.x, vb.y};
             }
             const Tri t = tri(bf.tw4, 256, J);
@@ -310,7 +311,7 @@ __device__ __forceinline__ void inv_passes(const S6c& z, const LargePlan& P, con
         for (u32 e = tid; e < (u32)(CC * CR); e += CNT) {
             const u64 o = (u64)(e / CC) * B + (u64)g * CC + e % CC;
             const ulonglong2 va = bf.za[o];
-            const uint2 vb = bf.zb[o];
+            const uint2 vb = kDual ? bf.zb[o] : make_uint2(0u, 0u);
             z.st(e, E{va.x, va.y, vb.x, vb.y});
         }
     }
@@ -361,8 +362,8 @@ __device__ __forceinline__ void inv_row_stage(const S6c& z, const LargePlan& P, 
                 const u64 j = j0 + 2 * cc;
                 const u64 bp1 = bitpos(p, ln, j + 1), bp2 = bitpos(p, ln, j + 2);
                 const i64 sub = (P.mode == LL && j == 0) ? 2 : 0;
-                d[2 * cc] = crt_digit(x0, y0, (u32)(bp1 - bp), mul, sub, c, bad, P.gf61 != 0);
-                d[2 * cc + 1] = crt_digit(x1, y1, (u32)(bp2 - bp1), mul, 0, c, bad, P.gf61 != 0);
+                d[2 * cc] = crt_digit(x0, y0, (u32)(bp1 - bp), mul, sub, c, bad, !kDual || P.gf61 != 0);
+                d[2 * cc + 1] = crt_digit(x1, y1, (u32)(bp2 - bp1), mul, 0, c, bad, !kDual || P.gf61 != 0);
                 bp = bp2;
             }
         }
@@ -547,6 +548,9 @@ cudaError_t cols_q_setup(const LargePlan& P) { return P.R == 1024u ? setup_shape
 // groups by arrival ticket
 bool cols_mid_supported(const LargePlan& P) { return cols_q_supported(P); }
 bool cols_mid_cooperative(const LargePlan& P) {
+#if M2_DUAL
+    if (P.gf61) return m2k_g61::cols_mid_cooperative(P);
+#endif
     if (!cols_q_supported(P)) return false;
     return P.R == 1024u ? mid_fits<1024>(P) : mid_fits<256>(P);
 }
@@ -568,4 +572,4 @@ cudaError_t launch_cols_mid(const LargePlan& P, const LargeBufs& b, cudaStream_t
     return P.R == 1024u ? launch_mid<1024>(P, b, s) : launch_mid<256>(P, b, s);
 }
 
-}  // namespace m2k
+}  // namespace M2K_NS

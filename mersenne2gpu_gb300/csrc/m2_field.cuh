@@ -11,10 +11,29 @@
 // coordinate is in [0, P31].  Twiddles are stored canonical ([0, P61]).
 // Helpers accept and return these ranges unless stated otherwise; rotl61 and
 // the CRT need [0, P61] and get it from full61 / fold61.
+//
+// Built twice: with M2_DUAL = 1 (the default, namespace m2d) for both fields,
+// and with M2_DUAL = 0 (namespace m2d61) for the GF(P61^2)-only layout, where
+// every GF(P31^2) coordinate is the constant 0: loads, stores, shuffles and
+// products of that half compile away (kDual).
 #pragma once
 #include <cstdint>
 
-namespace m2d {
+#ifndef M2_DUAL
+#define M2_DUAL 1
+#endif
+#if M2_DUAL
+#define M2D_NS m2d
+#else
+#define M2D_NS m2d61
+#endif
+
+namespace M2D_NS {
+
+// false in the GF(P61^2)-only build: the GF(P31^2) half is not computed
+constexpr bool kDual = M2_DUAL != 0;
+// a GF(P31^2) coordinate as the build carries it
+__device__ __forceinline__ unsigned int g31(unsigned int v) { return kDual ? v : 0u; }
 
 typedef unsigned long long u64;
 typedef unsigned int u32;
@@ -133,19 +152,22 @@ __device__ __forceinline__ E econjsub(const E& x, const E& y) { return E{sub61(x
 __device__ __forceinline__ E emul(const E& x, const E& w) {
     E r;
     cmul61(x.a, x.b, w.a, w.b, r.a, r.b);
-    cmul31(x.c, x.d, w.c, w.d, r.c, r.d);
+    if (kDual) cmul31(x.c, x.d, w.c, w.d, r.c, r.d);
+    else r.c = r.d = 0;
     return r;
 }
 __device__ __forceinline__ E emulconj(const E& x, const E& w) {
     E r;
     cmulconj61(x.a, x.b, w.a, w.b, r.a, r.b);
-    cmulconj31(x.c, x.d, w.c, w.d, r.c, r.d);
+    if (kDual) cmulconj31(x.c, x.d, w.c, w.d, r.c, r.d);
+    else r.c = r.d = 0;
     return r;
 }
 __device__ __forceinline__ E esqr(const E& x) {
     E r;
     csqr61(x.a, x.b, r.a, r.b);
-    csqr31(x.c, x.d, r.c, r.d);
+    if (kDual) csqr31(x.c, x.d, r.c, r.d);
+    else r.c = r.d = 0;
     return r;
 }
 
@@ -249,8 +271,8 @@ __device__ __forceinline__ E shfl_xor_e(const E& v, int m) {
     E r;
     r.a = __shfl_xor_sync(0xffffffffu, v.a, m);
     r.b = __shfl_xor_sync(0xffffffffu, v.b, m);
-    r.c = __shfl_xor_sync(0xffffffffu, v.c, m);
-    r.d = __shfl_xor_sync(0xffffffffu, v.d, m);
+    r.c = kDual ? __shfl_xor_sync(0xffffffffu, v.c, m) : 0u;
+    r.d = kDual ? __shfl_xor_sync(0xffffffffu, v.d, m) : 0u;
     return r;
 }
 
@@ -290,4 +312,4 @@ __device__ __forceinline__ i64 split_balanced64(i64 t, u32 w, i64& c) {
     return t - (c << w);
 }
 
-}  // namespace m2d
+}  // namespace M2D_NS

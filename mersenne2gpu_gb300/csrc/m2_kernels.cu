@@ -26,16 +26,19 @@
 #include "m2_kernels.cuh"
 #include "m2_field.cuh"
 
-using namespace m2d;
+using namespace M2D_NS;
 
-namespace m2k {
+namespace M2K_NS {
 
 namespace {
 
 struct SE {
     u64* a; u64* b; u32* c; u32* d;
-    __device__ __forceinline__ E ld(u32 i) const { return E{a[i], b[i], c[i], d[i]}; }
-    __device__ __forceinline__ void st(u32 i, const E& e) const { a[i] = e.a; b[i] = e.b; c[i] = e.c; d[i] = e.d; }
+    __device__ __forceinline__ E ld(u32 i) const { return E{a[i], b[i], kDual ? c[i] : 0u, kDual ? d[i] : 0u}; }
+    __device__ __forceinline__ void st(u32 i, const E& e) const {
+        a[i] = e.a; b[i] = e.b;
+        if (kDual) { c[i] = e.c; d[i] = e.d; }
+    }
 };
 __device__ __forceinline__ SE make_se(unsigned char* base, u32 ne) {
     return SE{(u64*)base, (u64*)base + ne, (u32*)(base + 16ull * ne), (u32*)(base + 16ull * ne) + ne};
@@ -50,8 +53,15 @@ __device__ __forceinline__ SE make_se(unsigned char* base, u32 ne) {
 __device__ __forceinline__ u32 swsm(u32 i) { return i ^ ((((i >> 4) * 5u) ^ (i >> 8)) & 15u); }
 struct SZ {
     u64* a; u64* b; u32* c; u32* d;
-    __device__ __forceinline__ E ld(u32 i) const { const u32 q = swsm(i); return E{a[q], b[q], c[q], d[q]}; }
-    __device__ __forceinline__ void st(u32 i, const E& e) const { const u32 q = swsm(i); a[q] = e.a; b[q] = e.b; c[q] = e.c; d[q] = e.d; }
+    __device__ __forceinline__ E ld(u32 i) const {
+        const u32 q = swsm(i);
+        return E{a[q], b[q], kDual ? c[q] : 0u, kDual ? d[q] : 0u};
+    }
+    __device__ __forceinline__ void st(u32 i, const E& e) const {
+        const u32 q = swsm(i);
+        a[q] = e.a; b[q] = e.b;
+        if (kDual) { c[q] = e.c; d[q] = e.d; }
+    }
     __device__ __forceinline__ u64& A(u32 i) const { return a[swsm(i)]; }
     __device__ __forceinline__ u64& Bv(u32 i) const { return b[swsm(i)]; }
 };
@@ -61,7 +71,7 @@ __device__ __forceinline__ SZ make_sz(unsigned char* base, u32 ne) {
 
 __device__ __forceinline__ E ldtw(const DTw* t, u32 i) {
     const u64* q = reinterpret_cast<const u64*>(t + i);
-    const u64 a = __ldg(q), b = __ldg(q + 1), cd = __ldg(q + 2);
+    const u64 a = __ldg(q), b = __ldg(q + 1), cd = kDual ? __ldg(q + 2) : 0ull;
     return E{a, b, (u32)cd, (u32)(cd >> 32)};
 }
 
@@ -69,7 +79,7 @@ __device__ __forceinline__ u64 bitpos(u32 p, int ln, u64 j) { return j ? ((((u64
 __device__ __forceinline__ u32 width_of(u32 p, int ln, u64 j) { return (u32)(bitpos(p, ln, j + 1) - bitpos(p, ln, j)); }
 
 __device__ __forceinline__ E weigh(i64 d0, i64 d1, u32 s061, u32 s161, u32 s031, u32 s131) {
-    return E{rotl61(digit_to61(d0), s061), rotl61(digit_to61(d1), s161), rotl31(digit_to31(d0), s031), rotl31(digit_to31(d1), s131)};
+    return E{rotl61(digit_to61(d0), s061), rotl61(digit_to61(d1), s161), g31(rotl31(digit_to31(d0), s031)), g31(rotl31(digit_to31(d1), s131))};
 }
 // multiplier 2^-(s + ln + 1) as a left rotation
 __device__ __forceinline__ u32 unrot61(u32 s, int ln) { const u32 t = (s + (u32)ln + 1u) % 61u; return t ? 61u - t : 0u; }
@@ -84,7 +94,7 @@ __device__ __forceinline__ i128 signed61(u64 a) {
 __device__ __forceinline__ void unweigh_crt(const E& v, u64 j, const unsigned char* w61, const unsigned char* w31, int ln,
                                             int mode, int gf61_only, i128& z0, i128& z1) {
     const u64 a = rotl61(fold61(v.a), unrot61(w61[j], ln)), b = rotl61(fold61(v.b), unrot61(w61[j + 1], ln));
-    if (gf61_only) {
+    if (!kDual || gf61_only) {
         z0 = signed61(a);
         z1 = signed61(b);
     } else {
@@ -375,7 +385,10 @@ const void* small_fn(bool fuse) { return fuse ? (const void*)k_small<true> : (co
 }  // namespace
 
 cudaError_t launch_small(const SmallTest* d_tests, int ntests, unsigned int h, int threads, unsigned int iters_override,
-                         cudaStream_t s, bool fuse) {
+                         cudaStream_t s, bool fuse, bool gf61) {
+#if M2_DUAL
+    if (gf61) return m2k_g61::launch_small(d_tests, ntests, h, threads, iters_override, s, fuse, true);
+#endif
     const size_t sm = small_smem_bytes(h, threads);
     cudaError_t e = cudaFuncSetAttribute(small_fn(fuse), cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_smem_limit(small_fn(fuse)));
     if (e != cudaSuccess) return e;
@@ -456,7 +469,7 @@ __global__ void __launch_bounds__(LTC, 2) k_cols_fwd(LargePlan P, LargeBufs bf) 
         const u64 e = (u64)t * B + (u64)g * C + cc;
         const E v = z.ld(l);
         bf.za[e] = make_ulonglong2(v.a, v.b);
-        bf.zb[e] = make_uint2(v.c, v.d);
+        if (kDual) bf.zb[e] = make_uint2(v.c, v.d);
     }
 }
 
@@ -477,7 +490,7 @@ __global__ void __launch_bounds__(LT, 4) k_rows(LargePlan P, LargeBufs bf) {
         const u32 sl = l / B, col = l % B;
         const u64 e = (u64)(sl ? t1 : t0) * B + col;
         const ulonglong2 va = bf.za[e];
-        const uint2 vb = bf.zb[e];
+        const uint2 vb = kDual ? bf.zb[e] : make_uint2(0u, 0u);
         z.st(l, E{va.x, va.y, vb.x, vb.y});
     }
     __syncthreads();
@@ -564,7 +577,7 @@ __global__ void __launch_bounds__(LT, 4) k_rows(LargePlan P, LargeBufs bf) {
         const u64 e = (u64)(sl ? t1 : t0) * B + col;
         const E v = z.ld(l);
         bf.za[e] = make_ulonglong2(v.a, v.b);
-        bf.zb[e] = make_uint2(v.c, v.d);
+        if (kDual) bf.zb[e] = make_uint2(v.c, v.d);
     }
 }
 
@@ -580,7 +593,7 @@ __global__ void __launch_bounds__(LTC, 2) k_cols_inv(LargePlan P, LargeBufs bf) 
         const u32 t = l / C, cc = l % C;
         const u64 e = (u64)t * B + (u64)g * C + cc;
         const ulonglong2 va = bf.za[e];
-        const uint2 vb = bf.zb[e];
+        const uint2 vb = kDual ? bf.zb[e] : make_uint2(0u, 0u);
         z.st(l, E{va.x, va.y, vb.x, vb.y});
     }
     __syncthreads();
@@ -624,6 +637,9 @@ size_t large_smem_rows(const LargePlan& P) { return 24ull * 2 * P.B; }
 #define M2_FOR_C(X) X(4) X(8) X(16)
 
 cudaError_t large_setup(const LargePlan& P) {
+#if M2_DUAL
+    if (P.gf61) return m2k_g61::large_setup(P);
+#endif
     cudaError_t e;
 #define M2_SET(CC)                                                                                          \
     if (P.C == CC) {                                                                                        \
@@ -641,6 +657,9 @@ cudaError_t large_setup(const LargePlan& P) {
 }
 
 cudaError_t launch_large_stage(const LargePlan& P, const LargeBufs& b, int stage, cudaStream_t s) {
+#if M2_DUAL
+    if (P.gf61) return m2k_g61::launch_large_stage(P, b, stage, s);
+#endif
     const size_t sc = large_smem_cols(P), sr = large_smem_rows(P);
     if (stage == STAGE_MID) return b.flags ? launch_cols_mid(P, b, s) : cudaErrorInvalidValue;
     if (stage != 1 && cols_q_supported(P)) return launch_cols_q(P, b, stage == 2, s);
@@ -675,6 +694,9 @@ unsigned long long large_stage_bytes(const LargePlan& P, int stage) {
 }
 
 cudaError_t launch_large_iteration(const LargePlan& P, const LargeBufs& b, cudaStream_t s) {
+#if M2_DUAL
+    if (P.gf61) return m2k_g61::launch_large_iteration(P, b, s);
+#endif
     for (int st = 0; st < LARGE_STAGES; ++st) {
         cudaError_t e = launch_large_stage(P, b, st, s);
         if (e != cudaSuccess) return e;
@@ -683,6 +705,9 @@ cudaError_t launch_large_iteration(const LargePlan& P, const LargeBufs& b, cudaS
 }
 
 cudaError_t launch_large_run(const LargePlan& P, const LargeBufs& b, unsigned k, bool fused, cudaStream_t s) {
+#if M2_DUAL
+    if (P.gf61) return m2k_g61::launch_large_run(P, b, k, fused, s);
+#endif
     cudaError_t e = cudaSuccess;
     if (k == 0) return e;
     if (!fused) {
@@ -695,4 +720,4 @@ cudaError_t launch_large_run(const LargePlan& P, const LargeBufs& b, unsigned k,
     return launch_large_stage(P, b, 2, s);
 }
 
-}  // namespace m2k
+}  // namespace M2K_NS

@@ -58,40 +58,8 @@ struct LargeBufs {
     unsigned long long* phase;
 };
 
-size_t small_smem_bytes(unsigned int h, int threads);
-int small_threads_for(unsigned int h);
-// iters_override != 0 replaces every test's iteration count for this launch;
-// fuse selects the kernel variant with the fused transform middle (every test
-// of the launch must have fuse_middle equal to it)
-cudaError_t launch_small(const SmallTest* d_tests, int ntests, unsigned int h, int threads, unsigned int iters_override,
-                         cudaStream_t s, bool fuse = false);
-// persistent grid: CTAs take test indices from *d_queue (zeroed by the caller)
-cudaError_t launch_small_persistent(const SmallTest* d_tests, int ntests, unsigned int h, int threads, int* d_queue,
-                                    int grid, cudaStream_t s, bool fuse = false);
-int small_ctas_per_sm(unsigned int h, int threads, bool fuse = false);
-
-size_t large_smem_cols(const LargePlan& P);
-size_t large_smem_rows(const LargePlan& P);
-cudaError_t large_setup(const LargePlan& P);   // sets max dynamic smem attributes
-cudaError_t launch_large_iteration(const LargePlan& P, const LargeBufs& b, cudaStream_t s);
 constexpr int LARGE_STAGES = 3;
 constexpr int STAGE_MID = 3;   // the fused inverse + forward column pass (k_cols_mid_q)
-// k squarings: fwd, rows, (mid, rows) x (k - 1), inv when fused, else k x (fwd, rows, inv)
-cudaError_t launch_large_run(const LargePlan& P, const LargeBufs& b, unsigned k, bool fused, cudaStream_t s);
-// quad-shuffle row pass (m2_rows.cu), used for row lengths 1024 and 2048
-bool rows_q_supported(const LargePlan& P);
-cudaError_t rows_q_setup(const LargePlan& P);
-cudaError_t launch_rows_q(const LargePlan& P, const LargeBufs& b, cudaStream_t s);
-// quad-shuffle column passes (m2_cols.cu), used for R = 1024 rows and C = 4
-bool cols_q_supported(const LargePlan& P);
-cudaError_t cols_q_setup(const LargePlan& P);
-cudaError_t launch_cols_q(const LargePlan& P, const LargeBufs& b, bool inverse, cudaStream_t s);
-bool cols_mid_supported(const LargePlan& P);     // the fused column kernel serves this plan
-bool cols_mid_cooperative(const LargePlan& P);   // ... with all G CTAs co-resident (cooperative launch)
-cudaError_t launch_cols_mid(const LargePlan& P, const LargeBufs& b, cudaStream_t s);
-cudaError_t launch_large_stage(const LargePlan& P, const LargeBufs& b, int stage, cudaStream_t s);
-const char* large_stage_name(int stage);
-unsigned long long large_stage_bytes(const LargePlan& P, int stage);
 
 // Throughput of 32x32->64-bit integer multiplies (mul.wide.u32 / mad.wide.u32)
 // on every SM: independent chains, returns products per second.
@@ -120,3 +88,22 @@ cudaError_t launch_balance(const unsigned long long* canon, long long* digits, u
                            unsigned long long n, unsigned int* bad, cudaStream_t s);
 
 }  // namespace m2k
+
+// The transform kernels are built twice (m2_field.cuh): M2_DUAL = 1 into
+// namespace m2k, M2_DUAL = 0 (GF(P61^2) alone) into m2k_g61.  A kernel build
+// sees only its own entry points, so that calls inside it resolve to them.
+#ifndef M2_DUAL
+#define M2_DUAL 1
+#endif
+#if M2_DUAL
+#define M2K_NS m2k
+namespace m2k {
+#include "m2_launch.inc"
+}  // namespace m2k
+#else
+#define M2K_NS m2k_g61
+#endif
+namespace m2k_g61 {
+using namespace m2k;
+#include "m2_launch.inc"
+}  // namespace m2k_g61

@@ -33,9 +33,9 @@
 #include "m2_field.cuh"
 #include "m2_kernels.cuh"
 
-using namespace m2d;
+using namespace M2D_NS;
 
-namespace m2k {
+namespace M2K_NS {
 
 namespace {
 
@@ -59,10 +59,11 @@ __device__ __forceinline__ u32 swz(u32 e) {
 struct S6 {
     u32 *al, *ah, *bl, *bh, *c, *d;
     __device__ __forceinline__ E ldp(u32 p) const {
-        return E{(u64)al[p] | ((u64)ah[p] << 32), (u64)bl[p] | ((u64)bh[p] << 32), c[p], d[p]};
+        return E{(u64)al[p] | ((u64)ah[p] << 32), (u64)bl[p] | ((u64)bh[p] << 32), kDual ? c[p] : 0u, kDual ? d[p] : 0u};
     }
     __device__ __forceinline__ void stp(u32 p, const E& v) const {
-        al[p] = (u32)v.a; ah[p] = (u32)(v.a >> 32); bl[p] = (u32)v.b; bh[p] = (u32)(v.b >> 32); c[p] = v.c; d[p] = v.d;
+        al[p] = (u32)v.a; ah[p] = (u32)(v.a >> 32); bl[p] = (u32)v.b; bh[p] = (u32)(v.b >> 32);
+        if (kDual) { c[p] = v.c; d[p] = v.d; }
     }
     __device__ __forceinline__ E ld(u32 e) const { return ldp(swz(e)); }
     __device__ __forceinline__ void st(u32 e, const E& v) const { stp(swz(e), v); }
@@ -74,11 +75,11 @@ __device__ __forceinline__ S6 make_s6(unsigned char* base, u32 ne) {
 
 __device__ __forceinline__ E ldw(const DTw* t, u64 i) {
     const u64* q = reinterpret_cast<const u64*>(t + i);
-    const u64 a = __ldg(q), b = __ldg(q + 1), cd = __ldg(q + 2);
+    const u64 a = __ldg(q), b = __ldg(q + 1), cd = kDual ? __ldg(q + 2) : 0ull;
     return E{a, b, (u32)cd, (u32)(cd >> 32)};
 }
 __device__ __forceinline__ u64 neg61(u64 x) { return P61 - x; }
-__device__ __forceinline__ u32 neg31(u32 x) { return P31 - x; }
+__device__ __forceinline__ u32 neg31(u32 x) { return g31(P31 - x); }
 // mirror-block twiddles (inputs canonical, outputs in [0, P61] / [0, P31])
 __device__ __forceinline__ E mir1(const E& r) { return E{r.b, r.a, r.d, r.c}; }                                 // i conj(r)
 __device__ __forceinline__ E mir2(const E& r) { return E{neg61(r.a), r.b, neg31(r.c), r.d}; }                  // -conj(r^2)
@@ -97,12 +98,12 @@ __device__ __forceinline__ Tri tri(const DTw* tw4, u64 S, u64 J, bool mir) {
 
 __device__ __forceinline__ E gload(const LargeBufs& bf, u64 e) {
     const ulonglong2 va = bf.za[e];
-    const uint2 vb = bf.zb[e];
+    const uint2 vb = kDual ? bf.zb[e] : make_uint2(0u, 0u);
     return E{va.x, va.y, vb.x, vb.y};
 }
 __device__ __forceinline__ void gstore(const LargeBufs& bf, u64 e, const E& v) {
     bf.za[e] = make_ulonglong2(v.a, v.b);
-    bf.zb[e] = make_uint2(v.c, v.d);
+    if (kDual) bf.zb[e] = make_uint2(v.c, v.d);
 }
 
 
@@ -397,4 +398,4 @@ cudaError_t launch_rows_q(const LargePlan& P, const LargeBufs& b, cudaStream_t s
     return cudaErrorInvalidValue;
 }
 
-}  // namespace m2k
+}  // namespace M2K_NS

@@ -156,11 +156,13 @@ def test_gf61_only_matches_dual_fields(m2, p, mode):
             assert a.res64() == b.res64(), p
 
 
-@pytest.mark.parametrize("p,n", [(2976221, 1 << 18), (18874367, 1 << 20)])
+@pytest.mark.parametrize("p,n", [(2976221, 1 << 18), (18874367, 1 << 20), (36700159, 1 << 21)])
 def test_gf61_only_three_pass_matches_dual_fields(m2, p, n):
-    """GF(P61^2)-only layouts on the three-pass path: the generic kernels
-    (n = 2^18: 256 x 512) and the quad-shuffle ones with the cooperative fused
-    column pass (n = 2^20: 256 x 2048) give the dual-field engine's residues."""
+    """GF(P61^2)-only layouts on the three-pass path (the kernel build without
+    the GF(P31^2) half): the generic kernels (n = 2^18: 256 x 512) and the
+    quad-shuffle ones with the cooperative fused column pass (n = 2^20:
+    256 x 2048; n = 2^21: 1024 x 1024 with the phase barrier) give the
+    dual-field engine's residues."""
     with m2.Engine(p, 1, fields=m2.FIELDS_GF61) as a, m2.Engine(p, 1) as b:
         assert a.info().path == m2.PATH_LARGE and a.info().n == n and b.info().n == n // 2
         for _ in range(2):
