@@ -149,8 +149,8 @@ struct m2_ctx {
     unsigned* d_flags = nullptr;
     bool fused = false;        // inverse and next forward column pass as one cooperative launch
     bool gf61 = false;         // GF(P61^2)-only transform (M2_FIELDS_GF61)
-    // GRAPH_ITERS iterations of the three-pass path captured once and replayed
-    cudaGraphExec_t graph = nullptr;
+    // GRAPH_ITERS[i] iterations of the three-pass path captured once and replayed
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
     bool graph_failed = false;
     // canonical digits and carry-propagation scratch (allocated on first read)
     unsigned long long* d_canon = nullptr;
@@ -172,15 +172,18 @@ template <class T> int dalloc(m2_ctx* c, T** p, size_t bytes) {
 size_t flags_bytes(const m2k::LargePlan& P) { return sizeof(unsigned) * ((size_t)P.G + 4); }
 
 
-// Iterations of the three-pass path per graph replay: 3 kernel nodes each.
-constexpr uint32_t GRAPH_ITERS = 50;
+// Iterations of the three-pass path per graph replay, long and short.  With the
+// fused column pass a replay of k squarings is 2k + 1 kernels (the forward
+// column pass opens it, the inverse one closes it), so the long graph spends
+// less on those two passes per squaring.
+constexpr uint32_t GRAPH_ITERS[2] = {500, 50};
 
-// Captures GRAPH_ITERS iterations on the context's stream into an executable
+// Captures GRAPH_ITERS[i] iterations on the context's stream into an executable
 // graph (once); replays cost one launch instead of 2 or 3 per iteration.  Not done
 // while the caller is capturing the stream itself, or if capture is refused
 // (the legacy default stream): launches are then issued one by one.
-bool ensure_graph(m2_ctx* c) {
-    if (c->graph) return true;
+bool ensure_graph(m2_ctx* c, int i) {
+    if (c->graph[i]) return true;
     if (c->graph_failed) return false;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(c->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
@@ -194,15 +197,15 @@ bool ensure_graph(m2_ctx* c) {
         return false;
     }
     cudaError_t e = cudaSuccess;
-    e = m2k::launch_large_run(c->plan, c->bufs, GRAPH_ITERS, c->fused, c->stream);
+    e = m2k::launch_large_run(c->plan, c->bufs, GRAPH_ITERS[i], c->fused, c->stream);
     const cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
-    if (e == cudaSuccess && ee == cudaSuccess && g && cudaGraphInstantiate(&c->graph, g, 0) == cudaSuccess) {
+    if (e == cudaSuccess && ee == cudaSuccess && g && cudaGraphInstantiate(&c->graph[i], g, 0) == cudaSuccess) {
         cudaGraphDestroy(g);
         return true;
     }
     if (g) cudaGraphDestroy(g);
     cudaGetLastError();
-    c->graph = nullptr;
+    c->graph[i] = nullptr;
     c->graph_failed = true;
     return false;
 }
@@ -451,8 +454,9 @@ int m2_iterate(m2_ctx* c, uint32_t k) {
         e = m2k::launch_small(c->d_test, 1, (unsigned)c->L.h, c->threads, k, c->stream, c->h_test.fuse_middle != 0, c->gf61);
     } else {
         uint32_t left = k;
-        if (left >= GRAPH_ITERS && ensure_graph(c))
-            for (; left >= GRAPH_ITERS && e == cudaSuccess; left -= GRAPH_ITERS) e = cudaGraphLaunch(c->graph, c->stream);
+        for (int i = 0; i < 2; ++i)
+            if (left >= GRAPH_ITERS[i] && ensure_graph(c, i))
+                for (; left >= GRAPH_ITERS[i] && e == cudaSuccess; left -= GRAPH_ITERS[i]) e = cudaGraphLaunch(c->graph[i], c->stream);
         if (left > 0 && e == cudaSuccess) e = m2k::launch_large_run(c->plan, c->bufs, left, c->fused, c->stream);
     }
     if (e != cudaSuccess) return fail_cuda("m2_iterate launch", e);
@@ -630,7 +634,8 @@ void m2_destroy(m2_ctx* c) {
                     c->d_canon, c->d_norm, c->d_flags};
     if (c->stream)
         for (void* b : bufs) if (b) cudaFreeAsync(b, c->stream);
-    if (c->graph) cudaGraphExecDestroy(c->graph);
+    for (cudaGraphExec_t g : c->graph)
+        if (g) cudaGraphExecDestroy(g);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -693,9 +698,15 @@ uint64_t m2_launches_for(m2_ctx* c, uint32_t k) {
     if (!c || k == 0) return 0;
     if (c->path == M2_PATH_SMALL) return 1ull;
     if (!c->fused) return (uint64_t)m2k::LARGE_STAGES * k;
-    // graph replays of GRAPH_ITERS squarings, then the rest in one sequence
-    const uint64_t chunks = c->graph_failed ? 0 : k / GRAPH_ITERS, rest = k - chunks * GRAPH_ITERS;
-    return chunks * (2ull * GRAPH_ITERS + 1) + (rest ? 2 * rest + 1 : 0);
+    // graph replays of GRAPH_ITERS[0] then GRAPH_ITERS[1] squarings, then the
+    // rest in one sequence
+    uint64_t left = k, n = 0;
+    for (int i = 0; i < 2 && !c->graph_failed; ++i) {
+        const uint64_t chunks = left / GRAPH_ITERS[i];
+        n += chunks * (2ull * GRAPH_ITERS[i] + 1);
+        left -= chunks * GRAPH_ITERS[i];
+    }
+    return n + (left ? 2 * left + 1 : 0);
 }
 
 int m2_measure_mul_peak(int device, double* products_per_s) {
