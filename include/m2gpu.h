@@ -224,7 +224,7 @@ int m2_measure_mul_peak(int device, double* products_per_s);
  * transform must satisfy 128 <= n <= 2^18 (2689 <= p <= 9437179), larger or
  * smaller exponents return M2_EUNSUPPORTED.  Every call shares that array:
  * calls whose work overlaps on the GPU race.  The first call on a device looks
- * up the array's device address; make it before any stream capture. */
+ * up the array's device address. */
 int m2_square_noalloc(uint32_t p, int mode, int64_t* digits, uint32_t iters, void* stream);
 
 /* ---------------- full carry propagation ----------------

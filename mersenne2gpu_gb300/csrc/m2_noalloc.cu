@@ -19,8 +19,7 @@
 // call rebuilds the tables and clears the carries it relies on, and two calls
 // whose work overlaps on the GPU (different streams, or different threads on
 // one device) race on it.  The first call on a device looks the array's device
-// address up (cudaGetSymbolAddress, with that device current); make that first
-// call before any stream capture on that device.
+// address up (cudaGetSymbolAddress, with that device current).
 #include "../../include/m2gpu.h"
 #include "m2_field.cuh"
 #include "m2_host.hpp"
