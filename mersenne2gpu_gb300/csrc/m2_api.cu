@@ -147,6 +147,7 @@ struct m2_ctx {
     ulonglong2* d_za = nullptr;
     uint2* d_zb = nullptr;
     unsigned* d_flags = nullptr;
+    uint2* d_aux = nullptr;    // per-element unweighting rotations and digit widths (m2k::LargeBufs::aux)
     bool fused = false;        // inverse and next forward column pass as one cooperative launch
     bool gf61 = false;         // GF(P61^2)-only transform (M2_FIELDS_GF61)
     // GRAPH_ITERS[i] iterations of the three-pass path captured once and replayed
@@ -431,6 +432,27 @@ int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts) {
         }
         raw->bufs = m2k::LargeBufs{raw->d_digits, raw->d_carries, raw->d_za, raw->d_zb, raw->d_w61, raw->d_w31,
                                    raw->tw.tw4, raw->tw.tc, raw->d_status, raw->d_flags};
+        if (m2k::cols_q_supported(P)) {
+            // the inverse column passes' per-element table: the rotation by
+            // 2^-(s + ln + 1) that unweights a digit of shift s (mod 61 and mod
+            // 31) and the digit widths
+            std::vector<uint2> aux(h);
+            const uint32_t ln1 = (uint32_t)raw->L.ln + 1;
+            auto un = [ln1](uint32_t s, uint32_t m) { const uint32_t t = (s + ln1) % m; return t ? m - t : 0u; };
+            for (u64 k = 0; k < h; ++k) {
+                const u64 j = 2 * k;
+                aux[k].x = un(raw->L.w61[j], 61) | (un(raw->L.w61[j + 1], 61) << 8) | (un(raw->L.w31[j], 31) << 16) |
+                           (un(raw->L.w31[j + 1], 31) << 24);
+                aux[k].y = (uint32_t)raw->L.width[j] | ((uint32_t)raw->L.width[j + 1] << 8);
+            }
+            if ((rc = dalloc(raw, &raw->d_aux, sizeof(uint2) * h))) { m2_destroy(c.release()); return rc; }
+            if (cudaMemcpyAsync(raw->d_aux, aux.data(), sizeof(uint2) * h, cudaMemcpyHostToDevice, raw->stream) != cudaSuccess ||
+                cudaStreamSynchronize(raw->stream) != cudaSuccess) {
+                m2_destroy(c.release());
+                return M2_ECUDA;
+            }
+            raw->bufs.aux = raw->d_aux;
+        }
         if (m2k::large_setup(P) != cudaSuccess) { m2_destroy(c.release()); return M2_EUNSUPPORTED; }
         raw->fused = m2k::cols_mid_supported(P);
         raw->plan.mid_tickets = (raw->fused && !m2k::cols_mid_cooperative(P)) ? 1u : 0u;
@@ -631,7 +653,7 @@ void m2_destroy(m2_ctx* c) {
     // stream-ordered frees: they follow the context's queued work and do not
     // wait for other streams; its stream is released once that work is done
     void* bufs[] = {c->d_w61, c->d_w31, c->d_status, c->d_digits, c->d_test, c->d_carries, c->d_za, c->d_zb,
-                    c->d_canon, c->d_norm, c->d_flags};
+                    c->d_canon, c->d_norm, c->d_flags, c->d_aux};
     if (c->stream)
         for (void* b : bufs) if (b) cudaFreeAsync(b, c->stream);
     for (cudaGraphExec_t g : c->graph)

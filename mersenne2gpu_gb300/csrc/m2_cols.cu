@@ -81,13 +81,6 @@ __device__ __forceinline__ u32 width_of(u32 p, int ln, u64 j) { return (u32)(bit
 __device__ __forceinline__ E weigh(i64 d0, i64 d1, u32 s061, u32 s161, u32 s031, u32 s131) {
     return E{rotl61(digit_to61(d0), s061), rotl61(digit_to61(d1), s161), g31(rotl31(digit_to31(d0), s031)), g31(rotl31(digit_to31(d1), s131))};
 }
-__device__ __forceinline__ u32 unrot61(u32 s, int ln) { const u32 t = (s + (u32)ln + 1u) % 61u; return t ? 61u - t : 0u; }
-__device__ __forceinline__ u32 unrot31(u32 s, int ln) { const u32 t = (s + (u32)ln + 1u) % 31u; return t ? 31u - t : 0u; }
-__device__ __forceinline__ bool fits64(i128 c) { const i128 hi = c >> 63; return hi == 0 || hi == -1; }
-
-// left rotation that multiplies by 2^-(s + ln + 1): s < 61 (31), ln + 1 <= 31
-__device__ __forceinline__ u32 unrot61f(u32 s, u32 ln1) { u32 t = s + ln1; t = t >= 61u ? t - 61u : t; return t ? 61u - t : 0u; }
-__device__ __forceinline__ u32 unrot31f(u32 s, u32 ln1) { u32 t = s + ln1; t = t >= 31u ? t - 31u : t; return t ? 31u - t : 0u; }
 
 // One digit of the carry: z = the signed convolution word with z == r61
 // (mod P61), z == r31 (mod P31), |z| < P61 P31 / 2 (Garner), then
@@ -329,43 +322,31 @@ __device__ __forceinline__ void inv_passes(const S6c& z, const LargePlan& P, con
     }
 }
 
-// inverse row stage: unweight, CRT, carry within the row segment of 8 digits;
+// inverse row stage: unweight (rotations from the per-element table), CRT,
+// carry within the row segment of 8 digits;
 // the digits go to global memory or back into the row's own shared slots, the
 // segment's carry out to global memory
 template <int CR, bool TO_SMEM>
 __device__ __forceinline__ void inv_row_stage(const S6c& z, const LargePlan& P, const LargeBufs& bf, u32 g) {
     constexpr int CNT = ColShape<CR>::CNT;
     const u32 B = P.B, G = P.G, tid = threadIdx.x;
-    const u32 p = P.p;
-    const int ln = P.ln;
 #pragma unroll 1
     for (u32 r = tid; r < (u32)CR; r += CNT) {
         const u64 e0 = (u64)r * B + (u64)g * CC, j0 = 2 * e0;
-        const uchar4* w61 = reinterpret_cast<const uchar4*>(bf.w61 + j0);
-        const uchar4* w31 = reinterpret_cast<const uchar4*>(bf.w31 + j0);
-        const u32 ln1 = (u32)ln + 1u, mul = (P.mode == PRP3) ? 3u : 1u;
-        // digit widths of the segment: bit positions ceil(p j / n) at j0 .. j0 + 8
-        u64 bp = bitpos(p, ln, j0);
+        const u32 mul = (P.mode == PRP3) ? 3u : 1u;
         i64 c = 0;
         u32 bad = 0;
         i64 d[2 * CC];
 #pragma unroll
-        for (int h2 = 0; h2 < 2; ++h2) {
-            const uchar4 a = w61[h2], b = w31[h2];
-            const u32 s61[4] = {a.x, a.y, a.z, a.w}, s31[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                const u32 cc = 2 * h2 + u;
-                const E v = z.ldp(swzc(r * CC) ^ cc);
-                const u64 x0 = rotl61(fold61(v.a), unrot61f(s61[2 * u], ln1)), x1 = rotl61(fold61(v.b), unrot61f(s61[2 * u + 1], ln1));
-                const u32 y0 = rotl31(v.c, unrot31f(s31[2 * u], ln1)), y1 = rotl31(v.d, unrot31f(s31[2 * u + 1], ln1));
-                const u64 j = j0 + 2 * cc;
-                const u64 bp1 = bitpos(p, ln, j + 1), bp2 = bitpos(p, ln, j + 2);
-                const i64 sub = (P.mode == LL && j == 0) ? 2 : 0;
-                d[2 * cc] = crt_digit(x0, y0, (u32)(bp1 - bp), mul, sub, c, bad, !kDual || P.gf61 != 0);
-                d[2 * cc + 1] = crt_digit(x1, y1, (u32)(bp2 - bp1), mul, 0, c, bad, !kDual || P.gf61 != 0);
-                bp = bp2;
-            }
+        for (int cc = 0; cc < CC; ++cc) {
+            // the element's unweighting rotations and digit widths
+            const uint2 t = bf.aux[e0 + cc];
+            const E v = z.ldp(swzc(r * CC) ^ (u32)cc);
+            const u64 x0 = rotl61(fold61(v.a), t.x & 0xffu), x1 = rotl61(fold61(v.b), (t.x >> 8) & 0xffu);
+            const u32 y0 = rotl31(v.c, (t.x >> 16) & 0xffu), y1 = rotl31(v.d, t.x >> 24);
+            const i64 sub = (P.mode == LL && j0 + 2 * cc == 0) ? 2 : 0;
+            d[2 * cc] = crt_digit(x0, y0, t.y & 0xffu, mul, sub, c, bad, !kDual || P.gf61 != 0);
+            d[2 * cc + 1] = crt_digit(x1, y1, (t.y >> 8) & 0xffu, mul, 0, c, bad, !kDual || P.gf61 != 0);
         }
         if (TO_SMEM) {
 #pragma unroll

@@ -56,6 +56,9 @@ struct LargeBufs {
     unsigned int* flags;      // G epoch flags of the fused column kernel, then its 64-bit ticket counter and
     unsigned long long* ticket;   // its 64-bit phase counter (zero-initialised)
     unsigned long long* phase;
+    // per element k (digits 2k, 2k+1): x = the two digits' unweighting rotations mod 61 (bytes 0, 1) and
+    // mod 31 (bytes 2, 3), y = their widths (bytes 0, 1); read by the quad-shuffle column passes
+    const uint2* aux;
 };
 
 constexpr int LARGE_STAGES = 3;
