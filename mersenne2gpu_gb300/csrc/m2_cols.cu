@@ -88,21 +88,19 @@ __device__ __forceinline__ E weigh(i64 d0, i64 d1, u32 s061, u32 s161, u32 s031,
 // The carry out is below 2^62 in magnitude for every exponent of the table,
 // so it is formed from the 128-bit t by a 64-bit funnel shift.  1 <= w <= 63.
 __device__ __forceinline__ i64 crt_digit(u64 r61, u32 r31, u32 w, u32 mul, i64 sub, i64& c, u32& bad, bool gf61) {
-    // canonical residues
-    r61 = (r61 == P61) ? 0 : r61;
+    // r61 in [0, P61], r31 in [0, P31]: either may be the non-canonical zero
     u64 lo, hi;
     if (gf61) {
         // GF(P61^2)-only layout: the word is the residue in (-P61/2, P61/2]
+        r61 = (r61 == P61) ? 0 : r61;
         const bool neg = r61 > (P61 >> 1);
         lo = neg ? r61 - P61 : r61;
         hi = neg ? ~0ull : 0ull;
     } else {
-    r31 = (r31 == P31) ? 0 : r31;
-    u64 u = r61 + (P61 - r31);                     // (r61 - r31) mod P61, < 2 P61
-    u = (u >= P61) ? u - P61 : u;
-    u += ((u << 31) & P61) | (u >> 30);            // + u 2^31 (a 61-bit rotation)
-    u = (u >= P61) ? u - P61 : u;                  // u = (r61 - r31) (2^31 + 1) mod P61
-    // L = u P31 + r31 = u 2^31 - u + r31 < P61 P31
+    u64 u = fold61(r61 + (P61 - r31));             // (r61 - r31) mod P61 in [0, P61] (the sum is below 2 P61)
+    u = fold61(u + (((u << 31) & P61) | (u >> 30)));   // u (2^31 + 1) mod P61 in [0, P61]: + u 2^31, a 61-bit rotation
+    // L = u P31 + r31 = u 2^31 - u + r31 <= P61 P31 + P31: a value of L at or
+    // above M = P61 P31 leaves L - M in [0, P31] below, the same word
     lo = u << 31; hi = u >> 33;
     const u64 lo2 = lo - u;
     hi -= (lo2 > lo);
