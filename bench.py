@@ -544,6 +544,8 @@ def run_gb300(a, dist: Dist) -> dict | None:
                    "plan": {"rows": info.rows, "row_len": info.row_len, "cols_per_cta": info.cols_per_cta,
                             "carry_span": info.span},
                    "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MB write), state stays L2-resident within a step",
+                   "parity_reads": "res64 read between the CUDA-event windows at every step boundary that is a GMP "
+                                   "checkpoint; the read's carry kernels are not counted in gpu_launches",
                    "parallelism": "replicas" if dist.world > 1 else "single"},
         "wall_s": wall,
         "gpu_launches": launches,
