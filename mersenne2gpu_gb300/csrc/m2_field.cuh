@@ -298,6 +298,56 @@ __device__ __forceinline__ i128 crt_signed(u64 r61, u32 r31) {
     return (L > (M >> 1)) ? (i128)L - (i128)M : (i128)L;
 }
 
+// One digit of the carry: z = the signed convolution word with z == r61
+// (mod P61), z == r31 (mod P31), |z| < P61 P31 / 2 (Garner), then
+// t = mul z + c + 2^(w-1), digit = (t mod 2^w) - 2^(w-1), carry out t >> w.
+// The carry out is below 2^62 in magnitude for every exponent of the table,
+// so it is formed from the 128-bit t by a 64-bit funnel shift.  1 <= w <= 63.
+__device__ __forceinline__ i64 crt_digit(u64 r61, u32 r31, u32 w, u32 mul, i64 sub, i64& c, u32& bad, bool gf61) {
+    // r61 in [0, P61], r31 in [0, P31]: either may be the non-canonical zero
+    u64 lo, hi;
+    if (gf61) {
+        // GF(P61^2)-only layout: the word is the residue in (-P61/2, P61/2]
+        r61 = (r61 == P61) ? 0 : r61;
+        const bool neg = r61 > (P61 >> 1);
+        lo = neg ? r61 - P61 : r61;
+        hi = neg ? ~0ull : 0ull;
+    } else {
+    u64 u = fold61(r61 + (P61 - r31));             // (r61 - r31) mod P61 in [0, P61] (the sum is below 2 P61)
+    u = fold61(u + (((u << 31) & P61) | (u >> 30)));   // u (2^31 + 1) mod P61 in [0, P61]: + u 2^31, a 61-bit rotation
+    // L = u P31 + r31 = u 2^31 - u + r31 <= P61 P31 + P31: a value of L at or
+    // above M = P61 P31 leaves L - M in [0, P31] below, the same word
+    lo = u << 31; hi = u >> 33;
+    const u64 lo2 = lo - u;
+    hi -= (lo2 > lo);
+    lo = lo2 + r31;
+    hi += (lo < lo2);
+    // signed: z = L - M when L > M/2 (M = P61 P31 = 2^92 - 2^61 - 2^31 + 1)
+    constexpr u64 MLO = 0xdfffffff80000001ull, MHI = 0x000000000fffffffull;   // M
+    constexpr u64 HLO = 0xefffffffc0000000ull, HHI = 0x0000000007ffffffull;   // (M - 1) / 2
+    if (hi > HHI || (hi == HHI && lo > HLO)) {
+        const u64 l2 = lo - MLO;
+        hi = hi - MHI - (l2 > lo);
+        lo = l2;
+    }
+    }
+    // t = mul z + c + half  (two's complement in hi:lo)
+    if (mul == 3) {
+        const u64 l3 = lo * 3;
+        hi = hi * 3 + __umul64hi(lo, 3);
+        lo = l3;
+    }
+    const i64 add = c - sub + ((i64)1 << (w - 1));
+    const u64 l4 = lo + (u64)add;
+    hi += (l4 < lo) + (u64)(add >> 63);            // sign-extend add into the high word
+    lo = l4;
+    // t >> w fits in 64 bits iff the high word above bit w-1 is pure sign
+    const i64 top = (i64)hi >> (w - 1);
+    bad |= (u32)(top != 0 && top != -1);
+    c = (i64)((hi << (64 - w)) | (lo >> w));
+    return (i64)(lo & ((1ull << w) - 1)) - ((i64)1 << (w - 1));
+}
+
 // Balanced split of t at width w: t = d + c 2^w with d in [-2^(w-1), 2^(w-1)).
 __device__ __forceinline__ i64 split_balanced(i128 t, u32 w, i128& c) {
     if (w == 0) { c = t; return 0; }

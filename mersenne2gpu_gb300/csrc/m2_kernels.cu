@@ -303,19 +303,30 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
         } else {
             const u32 D = (u32)(n / (u64)Tc);
             if (tid < (u32)Tc) {
-                i128 c = 0;
+                // the 64-bit two-word CRT and carry step (the column passes'):
+                // a carry that would leave 64 bits flags the state
+                i64 c = 0;
+                u32 bad = 0;
                 const u64 j0 = (u64)tid * D;
+                const u32 mul = (T.mode == PRP3) ? 3u : 1u;
+                const bool g61 = !kDual || T.gf61_only;
+                u64 bp = bitpos(p, ln, j0);
                 for (u32 u = 0; u < D; u += 2) {
                     const u32 k = (u32)((j0 + u) >> 1);
-                    i128 z0, z1;
-                    unweigh_crt(z.ld(k), 2ull * k, T.w61, T.w31, ln, T.mode, T.gf61_only, z0, z1);
-                    if (T.mode == LL && k == 0) z0 -= 2;
-                    const i64 d0 = split_balanced(z0 + c, width_of(p, ln, 2ull * k), c);
-                    const i64 d1 = split_balanced(z1 + c, width_of(p, ln, 2ull * k + 1), c);
+                    const u64 j = 2ull * k;
+                    const E v = z.ld(k);
+                    const u64 x0 = rotl61(fold61(v.a), unrot61(T.w61[j], ln)), x1 = rotl61(fold61(v.b), unrot61(T.w61[j + 1], ln));
+                    const u32 y0 = g61 ? 0u : rotl31(v.c, unrot31(T.w31[j], ln));
+                    const u32 y1 = g61 ? 0u : rotl31(v.d, unrot31(T.w31[j + 1], ln));
+                    const u64 bp1 = bitpos(p, ln, j + 1), bp2 = bitpos(p, ln, j + 2);
+                    const i64 sub = (T.mode == LL && j == 0) ? 2 : 0;
+                    const i64 d0 = crt_digit(x0, y0, (u32)(bp1 - bp), mul, sub, c, bad, g61);
+                    const i64 d1 = crt_digit(x1, y1, (u32)(bp2 - bp1), mul, 0, c, bad, g61);
+                    bp = bp2;
                     z.A(k) = (u64)d0; z.Bv(k) = (u64)d1;
                 }
-                if (!fits64(c)) atomicExch(T.status, ST_CARRY_RANGE);
-                cx[tid] = (i64)c;
+                if (bad) atomicExch(T.status, ST_CARRY_RANGE);
+                cx[tid] = c;
             }
             __syncthreads();
             if (tid < (u32)Tc) {
