@@ -105,7 +105,6 @@ __device__ __forceinline__ void unweigh_crt(const E& v, u64 j, const unsigned ch
     if (mode == PRP3) { z0 *= 3; z1 *= 3; }
 }
 
-__device__ __forceinline__ bool fits64(i128 c) { const i128 hi = c >> 63; return hi == 0 || hi == -1; }
 
 }  // namespace
 
@@ -623,22 +622,29 @@ __global__ void __launch_bounds__(LTC, 2) k_cols_inv(LargePlan P, LargeBufs bf) 
         __syncthreads();
         if (S == 1) break;
     }
+    // unweight, CRT and carry over the row segment (the 64-bit step of the
+    // quad-shuffle column passes; a carry that would leave 64 bits flags the state)
+    const u32 mul = (P.mode == PRP3) ? 3u : 1u;
+    const bool g61 = !kDual || P.gf61 != 0;
     for (u32 t = threadIdx.x; t < R; t += blockDim.x) {
         const u64 e0 = (u64)t * B + (u64)g * C;
-        i128 c = 0;
+        i64 c = 0;
+        u32 bad = 0;
+        u64 bp = bitpos(p, ln, 2 * e0);
 #pragma unroll
         for (int cc = 0; cc < C; ++cc) {
             const u64 e = e0 + cc, j = 2 * e;
-            i128 z0, z1;
-            unweigh_crt(z.ld(t * C + cc), j, bf.w61, bf.w31, ln, P.mode, (int)P.gf61, z0, z1);
-            if (P.mode == LL && e == 0) z0 -= 2;
-            const i64 d0 = split_balanced(z0 + c, width_of(p, ln, j), c);
-            const i64 d1 = split_balanced(z1 + c, width_of(p, ln, j + 1), c);
-            bf.digits[j] = d0;
-            bf.digits[j + 1] = d1;
+            const E v = z.ld(t * C + cc);
+            const u64 x0 = rotl61(fold61(v.a), unrot61(bf.w61[j], ln)), x1 = rotl61(fold61(v.b), unrot61(bf.w61[j + 1], ln));
+            const u32 y0 = g61 ? 0u : rotl31(v.c, unrot31(bf.w31[j], ln));
+            const u32 y1 = g61 ? 0u : rotl31(v.d, unrot31(bf.w31[j + 1], ln));
+            const u64 bp1 = bitpos(p, ln, j + 1), bp2 = bitpos(p, ln, j + 2);
+            bf.digits[j] = crt_digit(x0, y0, (u32)(bp1 - bp), mul, (P.mode == LL && e == 0) ? 2 : 0, c, bad, g61);
+            bf.digits[j + 1] = crt_digit(x1, y1, (u32)(bp2 - bp1), mul, 0, c, bad, g61);
+            bp = bp2;
         }
-        if (!fits64(c)) atomicExch(bf.status, ST_CARRY_RANGE);
-        bf.carries[(u64)t * G + g] = (i64)c;
+        if (bad) atomicExch(bf.status, ST_CARRY_RANGE);
+        bf.carries[(u64)t * G + g] = c;
     }
 }
 
