@@ -413,6 +413,12 @@ __global__ void __launch_bounds__(ColShape<CR>::CNT, 65536 / (64 * ColShape<CR>:
         }
     }
     __syncthreads();
+    // cooperative launch with R = 1024 (every CTA resident): the row pass, a
+    // programmatic dependent that waits for this grid's completion before it
+    // reads, may now take the SMs' free slots.  Measured: n = 2^21 0.2%
+    // faster; with R = 256 and rows of 2048 (n = 2^20) the early row CTAs
+    // crowded onto the few SMs with room, and the squaring took 36% longer.
+    if (!TK && CR == 1024) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     fwd_row_stage<CR, true>(z, P, bf, g);
     __syncthreads();
     fwd_passes<CR>(z, P, bf, g);
