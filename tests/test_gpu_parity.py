@@ -216,3 +216,41 @@ def test_small_path_carry_blocks_vs_oracle(m2, oracle_mod, p, cp):
     o = oracle_mod.Oracle(p, 1)
     o.iterate(100)
     _cmp(got, o.digits(), f"small p={p} -B {cp}")
+
+
+def test_graph_replays_vs_oracle(m2, oracle_mod):
+    """m2_iterate replays captured graphs of 500 and of 50 squarings and
+    launches the rest directly: 551 = 500 + 50 + 1 and then 1049 = 2 x 500 + 49
+    squarings end on the oracle's digits (generic three-pass kernels)."""
+    p = 132049
+    with m2.Engine(p, 1, path=m2.PATH_LARGE) as e:
+        e.iterate(551)
+        first = e.digits()
+        e.iterate(1049)
+        got = e.digits()
+    o = oracle_mod.Oracle(p, 1)
+    o.iterate(551)
+    _cmp(first, o.digits(), f"p={p} after 551")
+    o.iterate(1049)
+    _cmp(got, o.digits(), f"p={p} after 1600")
+
+
+def test_graph_replays_match_direct_launches(m2):
+    """The quad-shuffle kernels with the cooperative fused column pass (n =
+    2^19): 1049 squarings replayed as two graphs of 500 and 49 launched
+    directly end on the same digits as the same squarings launched directly
+    in runs of 49 or fewer (each run checked against the oracle elsewhere),
+    and the launch count follows the replays (2k + 1 kernels per run of k)."""
+    p = 18874367
+    with m2.Engine(p, 1, path=m2.PATH_LARGE) as a, m2.Engine(p, 1, path=m2.PATH_LARGE) as b:
+        assert a.info().fused_cols == 1
+        assert a.launches_for(1049) == 2 * (2 * 500 + 1) + (2 * 49 + 1)
+        assert a.launches_for(551) == (2 * 500 + 1) + (2 * 50 + 1) + (2 * 1 + 1)
+        a.iterate(1049)
+        left = 1049
+        while left:
+            k = min(left, 49)
+            b.iterate(k)
+            left -= k
+        _cmp(a.digits(), b.digits(), f"p={p} graphs against direct launches")
+        assert a.info().iteration == b.info().iteration == 1049
