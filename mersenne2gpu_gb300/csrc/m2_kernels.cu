@@ -213,9 +213,10 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
         // last step of an even log2 h runs there)
         const u32 s4last = (fuse && !odd) ? s4max / 4 : s4max;
         for (u32 S = 1; S <= s4last && s4last; S *= 4) {
-            const u32 M = h / S, Q = M >> 2;
+            // h, S and Q are powers of two: block and offset by shift and mask
+            const u32 lq = (u32)L - (31u - __clz(S)) - 2u, Q = 1u << lq, M = Q << 2;
             for (u32 b = tid; b < h / 4; b += nt) {
-                const u32 j = b / Q, i = b % Q, base = j * M + i;
+                const u32 j = b >> lq, i = b & (Q - 1u), base = j * M + i;
                 E x0 = z.ld(base), x1 = z.ld(base + Q), x2 = z.ld(base + 2 * Q), x3 = z.ld(base + 3 * Q);
                 const u32 ti = 3 * (S + j);
                 if (S == 1) dif4_1(x0, x1, x2, x3);   // the first level: root 1
@@ -262,9 +263,9 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
             __syncthreads();
         }
         for (u32 S = s4last; S >= 1 && s4last; S /= 4) {
-            const u32 M = h / S, Q = M >> 2;
+            const u32 lq = (u32)L - (31u - __clz(S)) - 2u, Q = 1u << lq, M = Q << 2;
             for (u32 b = tid; b < h / 4; b += nt) {
-                const u32 j = b / Q, i = b % Q, base = j * M + i;
+                const u32 j = b >> lq, i = b & (Q - 1u), base = j * M + i;
                 E x0 = z.ld(base), x1 = z.ld(base + Q), x2 = z.ld(base + 2 * Q), x3 = z.ld(base + 3 * Q);
                 const u32 ti = 3 * (S + j);
                 if (S == 1) dit4_1(x0, x1, x2, x3);
@@ -461,9 +462,10 @@ __global__ void __launch_bounds__(LTC, 2) k_cols_fwd(LargePlan P, LargeBufs bf) 
     }
     __syncthreads();
     for (u32 S = 1; S < R; S *= 4) {
-        const u32 M = R / S, Q = M >> 2;
+        // R, S and Q are powers of two: block and offset by shift and mask
+        const u32 M = R / S, Q = M >> 2, lq = 31u - __clz(Q);
         for (u32 b = threadIdx.x; b < NE / 4; b += blockDim.x) {
-            const u32 cc = b % C, rho = b / C, j = rho / Q, i = rho % Q;
+            const u32 cc = b % C, rho = b / C, j = rho >> lq, i = rho & (Q - 1u);
             const u32 r0 = j * M + i;
             const u32 i0 = r0 * C + cc, i1 = (r0 + Q) * C + cc, i2 = (r0 + 2 * Q) * C + cc, i3 = (r0 + 3 * Q) * C + cc;
             E x0 = z.ld(i0), x1 = z.ld(i1), x2 = z.ld(i2), x3 = z.ld(i3);
@@ -504,12 +506,13 @@ __global__ void __launch_bounds__(LT, 4) k_rows(LargePlan P, LargeBufs bf) {
         z.st(l, E{va.x, va.y, vb.x, vb.y});
     }
     __syncthreads();
-    const u32 per4 = B / 4;
+    // B, per4, Mloc and Q are powers of two: shifts and masks
+    const u32 per4 = B / 4, lp4 = 31u - __clz(per4);
     u32 S = P.R, Mloc = B;
     for (; Mloc >= 4; S *= 4, Mloc /= 4) {
-        const u32 Q = Mloc >> 2, nb = B / Mloc;
+        const u32 Q = Mloc >> 2, nb = B / Mloc, lq = 31u - __clz(Q);
         for (u32 b = threadIdx.x; b < 2 * per4; b += blockDim.x) {
-            const u32 sl = b / per4, rho = b % per4, j = rho / Q, i = rho % Q;
+            const u32 sl = b >> lp4, rho = b & (per4 - 1u), j = rho >> lq, i = rho & (Q - 1u);
             const u32 base = sl * B + j * Mloc + i;
             const u32 J = (sl ? t1 : t0) * nb + j;
             E x0 = z.ld(base), x1 = z.ld(base + Q), x2 = z.ld(base + 2 * Q), x3 = z.ld(base + 3 * Q);
@@ -569,9 +572,9 @@ __global__ void __launch_bounds__(LT, 4) k_rows(LargePlan P, LargeBufs bf) {
     }
     // inverse radix-4 steps in reverse order
     for (S /= 4, Mloc = odd ? 8 : 4; Mloc <= B && S >= P.R; S /= 4, Mloc *= 4) {
-        const u32 Q = Mloc >> 2, nb = B / Mloc;
+        const u32 Q = Mloc >> 2, nb = B / Mloc, lq = 31u - __clz(Q);
         for (u32 b = threadIdx.x; b < 2 * per4; b += blockDim.x) {
-            const u32 sl = b / per4, rho = b % per4, j = rho / Q, i = rho % Q;
+            const u32 sl = b >> lp4, rho = b & (per4 - 1u), j = rho >> lq, i = rho & (Q - 1u);
             const u32 base = sl * B + j * Mloc + i;
             const u32 J = (sl ? t1 : t0) * nb + j;
             E x0 = z.ld(base), x1 = z.ld(base + Q), x2 = z.ld(base + 2 * Q), x3 = z.ld(base + 3 * Q);
@@ -608,9 +611,9 @@ __global__ void __launch_bounds__(LTC, 2) k_cols_inv(LargePlan P, LargeBufs bf) 
     }
     __syncthreads();
     for (u32 S = R / 4; S >= 1; S /= 4) {
-        const u32 M = R / S, Q = M >> 2;
+        const u32 M = R / S, Q = M >> 2, lq = 31u - __clz(Q);
         for (u32 b = threadIdx.x; b < NE / 4; b += blockDim.x) {
-            const u32 cc = b % C, rho = b / C, j = rho / Q, i = rho % Q;
+            const u32 cc = b % C, rho = b / C, j = rho >> lq, i = rho & (Q - 1u);
             const u32 r0 = j * M + i;
             const u32 i0 = r0 * C + cc, i1 = (r0 + Q) * C + cc, i2 = (r0 + 2 * Q) * C + cc, i3 = (r0 + 3 * Q) * C + cc;
             E x0 = z.ld(i0), x1 = z.ld(i1), x2 = z.ld(i2), x3 = z.ld(i3);
