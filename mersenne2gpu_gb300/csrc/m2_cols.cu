@@ -138,7 +138,7 @@ __device__ __forceinline__ void fwd_row_stage(const S6c& z, const LargePlan& P, 
 #pragma unroll 1
     for (u32 r = tid; r < (u32)CR; r += CNT) {
         const u64 s = (u64)r * G + g;
-        const u64 sp = (s + RG - 1) % RG;
+        const u64 sp = s ? s - 1 : RG - 1;   // the segment before (the last one for segment 0)
         i64 c = FROM_SMEM ? (i64)__ldcg(reinterpret_cast<const long long*>(bf.carries + sp)) : bf.carries[sp];
         const u64 j0 = 2 * ((u64)r * B + (u64)g * CC);
         i64 d[2 * CC];

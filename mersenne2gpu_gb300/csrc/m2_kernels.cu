@@ -330,7 +330,7 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
             }
             __syncthreads();
             if (tid < (u32)Tc) {
-                i64 c = cx[(tid + (u32)Tc - 1u) % (u32)Tc];
+                i64 c = cx[tid ? tid - 1u : (u32)Tc - 1u];
                 const u64 j0 = (u64)tid * D;
                 for (int u = 0; u <= T.span; ++u) {
                     const u64 j = j0 + (u64)u;
@@ -443,7 +443,7 @@ __global__ void __launch_bounds__(LTC, 2) k_cols_fwd(LargePlan P, LargeBufs bf) 
     const int ln = P.ln;
     for (u32 t = threadIdx.x; t < R; t += blockDim.x) {
         const u64 s = (u64)t * G + g;
-        i64 c = bf.carries[(s + RG - 1) % RG];
+        i64 c = bf.carries[s ? s - 1 : RG - 1];   // the segment before (the last one for segment 0)
         const u64 e0 = (u64)t * B + (u64)g * C;
         const u64 j0 = 2 * e0;
         i64 d[2 * C];
@@ -487,7 +487,7 @@ __global__ void __launch_bounds__(LTC, 2) k_cols_fwd(LargePlan P, LargeBufs bf) 
 
 __global__ void __launch_bounds__(LT, 4) k_rows(LargePlan P, LargeBufs bf) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const u32 B = P.B, NE = 2 * B;
+    const u32 B = P.B, NE = 2 * B, lb = 31u - __clz(B);   // B is a power of two
     const SE z = make_se(smem, NE);
     const u32 pi = blockIdx.x;
     u32 t0, t1;
@@ -499,7 +499,7 @@ __global__ void __launch_bounds__(LT, 4) k_rows(LargePlan P, LargeBufs bf) {
         t1 = (2u << e) - 1u - a;
     }
     for (u32 l = threadIdx.x; l < NE; l += blockDim.x) {
-        const u32 sl = l / B, col = l % B;
+        const u32 sl = l >> lb, col = l & (B - 1u);
         const u64 e = (u64)(sl ? t1 : t0) * B + col;
         const ulonglong2 va = bf.za[e];
         const uint2 vb = kDual ? bf.zb[e] : make_uint2(0u, 0u);
@@ -586,7 +586,7 @@ __global__ void __launch_bounds__(LT, 4) k_rows(LargePlan P, LargeBufs bf) {
         if (S == P.R) break;
     }
     for (u32 l = threadIdx.x; l < NE; l += blockDim.x) {
-        const u32 sl = l / B, col = l % B;
+        const u32 sl = l >> lb, col = l & (B - 1u);
         const u64 e = (u64)(sl ? t1 : t0) * B + col;
         const E v = z.ld(l);
         bf.za[e] = make_ulonglong2(v.a, v.b);
