@@ -278,11 +278,10 @@ __device__ __forceinline__ E shfl_xor_e(const E& v, int m) {
 
 // ---------------- digits <-> field ----------------
 __device__ __forceinline__ u64 digit_to61(i64 d) { return d >= 0 ? (u64)d : P61 - (u64)(-d); }
-__device__ __forceinline__ u32 digit_to31(i64 d) {
-    const u64 m = (u64)(d >= 0 ? d : -d);
-    const u32 r = red31(m);
-    return d >= 0 ? r : (P31 ^ r);
-}
+// d + P31 2^32 (a multiple of P31, 2^63 - 2^32) is a non-negative 64-bit
+// value for every digit and pending carry (|d| < 2^62), so one reduction
+// gives d mod P31 without the sign branches
+__device__ __forceinline__ u32 digit_to31(i64 d) { return red31((u64)d + ((u64)P31 << 32)); }
 __device__ __forceinline__ u64 canon61(u64 x) { return x == P61 ? 0 : x; }
 __device__ __forceinline__ u32 canon31(u32 x) { return x == P31 ? 0 : x; }
 
