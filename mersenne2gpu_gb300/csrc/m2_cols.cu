@@ -76,15 +76,6 @@ __device__ __forceinline__ Tri tri(const DTw* tw4, u64 S, u64 J) {
     return Tri{ldw(tw4, base), ldw(tw4, base + 1), ldw(tw4, base + 2)};
 }
 
-// width of digit j, ceil(p (j+1) / n) - ceil(p j / n) with n = 2^ln: for
-// j >= 1 it is q + [((p j - 1) mod n) + (p mod n) >= n], the remainder taken
-// in 32-bit arithmetic (its low ln bits are exact); digit 0 has q + [p mod n != 0]
-__device__ __forceinline__ u32 width_of(u32 p, int ln, u64 j) {
-    const u32 nm = (1u << ln) - 1u, pm = p & nm, q = p >> ln;
-    if (j == 0) return q + (pm != 0u);
-    const u32 r = ((u32)j * pm - 1u) & nm;
-    return q + ((r + pm) >> ln);
-}
 __device__ __forceinline__ E weigh(i64 d0, i64 d1, u32 s061, u32 s161, u32 s031, u32 s131) {
     return E{rotl61(digit_to61(d0), s061), rotl61(digit_to61(d1), s161), g31(rotl31(digit_to31(d0), s031)), g31(rotl31(digit_to31(d1), s131))};
 }

@@ -297,6 +297,15 @@ __device__ __forceinline__ i128 crt_signed(u64 r61, u32 r31) {
     return (L > (M >> 1)) ? (i128)L - (i128)M : (i128)L;
 }
 
+// width of digit j, ceil(p (j+1) / n) - ceil(p j / n) with n = 2^ln: for
+// j >= 1 it is q + [((p j - 1) mod n) + (p mod n) >= n], the remainder taken
+// in 32-bit arithmetic (its low ln bits are exact); digit 0 has q + [p mod n != 0]
+__device__ __forceinline__ u32 width_of(u32 p, int ln, u64 j) {
+    const u32 nm = (1u << ln) - 1u, pm = p & nm, q = p >> ln;
+    if (j == 0) return q + (pm != 0u);
+    const u32 r = ((u32)j * pm - 1u) & nm;
+    return q + ((r + pm) >> ln);
+}
 // One digit of the carry: z = the signed convolution word with z == r61
 // (mod P61), z == r31 (mod P31), |z| < P61 P31 / 2 (Garner), then
 // t = mul z + c + 2^(w-1), digit = (t mod 2^w) - 2^(w-1), carry out t >> w.

@@ -75,8 +75,6 @@ __device__ __forceinline__ E ldtw(const DTw* t, u32 i) {
     return E{a, b, (u32)cd, (u32)(cd >> 32)};
 }
 
-__device__ __forceinline__ u64 bitpos(u32 p, int ln, u64 j) { return j ? ((((u64)p * j) - 1) >> ln) + 1 : 0; }
-__device__ __forceinline__ u32 width_of(u32 p, int ln, u64 j) { return (u32)(bitpos(p, ln, j + 1) - bitpos(p, ln, j)); }
 
 __device__ __forceinline__ E weigh(i64 d0, i64 d1, u32 s061, u32 s161, u32 s031, u32 s131) {
     return E{rotl61(digit_to61(d0), s061), rotl61(digit_to61(d1), s161), g31(rotl31(digit_to31(d0), s031)), g31(rotl31(digit_to31(d1), s131))};
@@ -310,7 +308,6 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
                 const u64 j0 = (u64)tid * D;
                 const u32 mul = (T.mode == PRP3) ? 3u : 1u;
                 const bool g61 = !kDual || T.gf61_only;
-                u64 bp = bitpos(p, ln, j0);
                 for (u32 u = 0; u < D; u += 2) {
                     const u32 k = (u32)((j0 + u) >> 1);
                     const u64 j = 2ull * k;
@@ -318,11 +315,9 @@ __device__ __forceinline__ void run_small(const SmallTest& T, u32 h, u32 iters, 
                     const u64 x0 = rotl61(fold61(v.a), unrot61(T.w61[j], ln)), x1 = rotl61(fold61(v.b), unrot61(T.w61[j + 1], ln));
                     const u32 y0 = g61 ? 0u : rotl31(v.c, unrot31(T.w31[j], ln));
                     const u32 y1 = g61 ? 0u : rotl31(v.d, unrot31(T.w31[j + 1], ln));
-                    const u64 bp1 = bitpos(p, ln, j + 1), bp2 = bitpos(p, ln, j + 2);
                     const i64 sub = (T.mode == LL && j == 0) ? 2 : 0;
-                    const i64 d0 = crt_digit(x0, y0, (u32)(bp1 - bp), mul, sub, c, bad, g61);
-                    const i64 d1 = crt_digit(x1, y1, (u32)(bp2 - bp1), mul, 0, c, bad, g61);
-                    bp = bp2;
+                    const i64 d0 = crt_digit(x0, y0, width_of(p, ln, j), mul, sub, c, bad, g61);
+                    const i64 d1 = crt_digit(x1, y1, width_of(p, ln, j + 1), mul, 0, c, bad, g61);
                     z.A(k) = (u64)d0; z.Bv(k) = (u64)d1;
                 }
                 if (bad) atomicExch(T.status, ST_CARRY_RANGE);
@@ -633,7 +628,6 @@ __global__ void __launch_bounds__(LTC, 2) k_cols_inv(LargePlan P, LargeBufs bf) 
         const u64 e0 = (u64)t * B + (u64)g * C;
         i64 c = 0;
         u32 bad = 0;
-        u64 bp = bitpos(p, ln, 2 * e0);
 #pragma unroll
         for (int cc = 0; cc < C; ++cc) {
             const u64 e = e0 + cc, j = 2 * e;
@@ -641,10 +635,8 @@ __global__ void __launch_bounds__(LTC, 2) k_cols_inv(LargePlan P, LargeBufs bf) 
             const u64 x0 = rotl61(fold61(v.a), unrot61(bf.w61[j], ln)), x1 = rotl61(fold61(v.b), unrot61(bf.w61[j + 1], ln));
             const u32 y0 = g61 ? 0u : rotl31(v.c, unrot31(bf.w31[j], ln));
             const u32 y1 = g61 ? 0u : rotl31(v.d, unrot31(bf.w31[j + 1], ln));
-            const u64 bp1 = bitpos(p, ln, j + 1), bp2 = bitpos(p, ln, j + 2);
-            bf.digits[j] = crt_digit(x0, y0, (u32)(bp1 - bp), mul, (P.mode == LL && e == 0) ? 2 : 0, c, bad, g61);
-            bf.digits[j + 1] = crt_digit(x1, y1, (u32)(bp2 - bp1), mul, 0, c, bad, g61);
-            bp = bp2;
+            bf.digits[j] = crt_digit(x0, y0, width_of(p, ln, j), mul, (P.mode == LL && e == 0) ? 2 : 0, c, bad, g61);
+            bf.digits[j + 1] = crt_digit(x1, y1, width_of(p, ln, j + 1), mul, 0, c, bad, g61);
         }
         if (bad) atomicExch(bf.status, ST_CARRY_RANGE);
         bf.carries[(u64)t * G + g] = c;
