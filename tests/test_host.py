@@ -125,3 +125,36 @@ def test_cli_gf61_first_line_without_gpu(m2):
     r = subprocess.run([_cli(), "216091", "prp", "--gf61"], capture_output=True, text=True)
     assert r.stdout.splitlines()[0] == "p=216091, ln=14, transform=8192 (n=16384)"
     assert r.returncode == 1
+
+
+@pytest.mark.parametrize("p", [3, 7, 31, 127, 9941, 132049, 2976221, 18874367, 57885161, 115640321])
+def test_carry_width_rule_matches_layout(m2, p):
+    """The kernels' carry loops take digit j's width as q + [((p j - 1) mod n)
+    + (p mod n) >= n] (q + [p mod n != 0] for j = 0), the remainder formed in
+    32-bit arithmetic; it must equal the layout's ceil(p (j+1) / n) -
+    ceil(p j / n) for every digit, in both field layouts."""
+    for fields in (m2.FIELDS_DUAL, m2.FIELDS_GF61):
+        ln, n, widths = m2.layout(p, fields)
+        nm, pm, q = n - 1, p & (n - 1), p >> ln
+        j = np.arange(n, dtype=np.uint64)
+        r = ((j * np.uint64(pm) - np.uint64(1)) & np.uint64(0xFFFFFFFF)) & np.uint64(nm)
+        w = np.uint64(q) + ((r + np.uint64(pm)) >> np.uint64(ln))
+        w[0] = q + (1 if pm else 0)
+        assert np.array_equal(w.astype(np.uint8), widths), (p, fields)
+
+
+def test_digit_to_p31_rule():
+    """A signed digit or pending carry d (|d| < 2^62) reaches GF(P31) as
+    (d + P31 2^32) mod P31 through one unsigned 64-bit reduction."""
+    P31 = (1 << 31) - 1
+
+    def red31(x):
+        r = (x & P31) + (x >> 31)
+        s = ((r & P31) + (r >> 31)) & 0xFFFFFFFF
+        return min(s, (s - P31) & 0xFFFFFFFF)
+
+    rng = np.random.default_rng(3)
+    ds = [0, 1, -1, P31, -P31, (1 << 62) - 1, -(1 << 62) + 1] + [int(x) for x in rng.integers(-(1 << 62), 1 << 62, 2000)]
+    for d in ds:
+        got = red31((d + (P31 << 32)) & ((1 << 64) - 1))
+        assert 0 <= got <= P31 and got % P31 == d % P31, d
