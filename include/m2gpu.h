@@ -91,7 +91,10 @@ typedef struct {
 } m2_info_t;
 
 /* Replaces main()'s setup (mersenne2_gpu.cpp:3727-4028): exponent -> transform,
- * tables, buffers, x0 = 4 (LL) / 3 (PRP, PRP3) (mersenne2_gpu.cpp:3908). */
+ * tables, buffers, x0 = 4 (LL) / 3 (PRP, PRP3) (mersenne2_gpu.cpp:3908).
+ * Transforms up to n = 2^23 digits: p <= 285212671 with both fields,
+ * p <= 150994943 with M2_FIELDS_GF61; larger exponents return M2_EUNSUPPORTED
+ * (a row of the three-pass plan would no longer fit one CTA's shared memory). */
 int m2_create(m2_ctx** out, uint32_t p, int mode, const m2_opts* opts);
 
 /* Replaces k rounds of enqueue_plan(iter_plan); enqueue_plan(post_plan);

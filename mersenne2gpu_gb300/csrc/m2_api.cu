@@ -275,6 +275,11 @@ bool plan_large(const m2::Layout& L, int span, uint32_t carry_pairs, m2k::LargeP
     while (2 * C < (uint32_t)span + 1 && C < 16) C <<= 1;
     if (2 * C < (uint32_t)span + 1 || C > P.B) return false;
     P.C = C; P.G = P.B / C;
+    // a row pair and a column group must each fit one CTA's shared memory
+    // (227 KiB on this GPU): rows of up to 4096 elements, n <= 2^23 digits
+    // (p <= 285212671 with both fields, 150994943 with GF(P61^2) alone)
+    constexpr uint64_t kSmem = 227ull * 1024;
+    if (24ull * 2 * P.B > kSmem || 24ull * P.C * P.R > kSmem) return false;
     return true;
 }
 

@@ -254,3 +254,30 @@ def test_graph_replays_match_direct_launches(m2):
             left -= k
         _cmp(a.digits(), b.digits(), f"p={p} graphs against direct launches")
         assert a.info().iteration == b.info().iteration == 1049
+
+
+def test_n2_23_vs_oracle_and_largest_size(m2, oracle_mod):
+    """n = 2^23, the largest transform the three-pass plan holds (rows of 4096
+    elements in one CTA's shared memory; p <= 285212671): a few squarings
+    against the oracle, the GF(P61^2)-only layout at the same n against the
+    dual engine, and the first exponent past it refused at creation."""
+    p = 200000033
+    _, n, w = m2.layout(p)
+    rng = np.random.default_rng(23)
+    start = (rng.integers(0, 1 << 62, n, dtype=np.uint64) & ((np.uint64(1) << w.astype(np.uint64)) - np.uint64(1)))
+    with m2.Engine(p, 1) as e:
+        assert e.info().n == 1 << 23 and e.info().row_len == 4096
+        e.set_digits(start, 0)                # a full-size residue
+        e.iterate(3)
+        got = e.digits()
+    o = oracle_mod.Oracle(p, 1)
+    o.set_digits(start, 0)
+    o.iterate(3)
+    _cmp(got, o.digits(), f"p={p} n=2^23")
+    with m2.Engine(115640321, 1, fields=m2.FIELDS_GF61) as a, m2.Engine(115640321, 1) as b:
+        assert a.info().n == 1 << 23
+        a.iterate(600)
+        b.iterate(600)
+        assert a.res64() == b.res64()
+    with pytest.raises(m2.M2Error, match=r"\(-6\)"):
+        m2.Engine(285212677, 1)     # n = 2^24
